@@ -1,0 +1,343 @@
+"""Benchmark of the single-engine hourly tick (agent-hours/s).
+
+Workload: the 1,000,000-agent / 2,500-grid run of 4,800 hours (small pox; 50 exposed;
+Lockdown at 1,000 infections with 10% essential workers; vaccination of 20% of the
+susceptible at hour 2,400; hospital build at 70% occupancy) -- tests/golden/c2_small_pox_1m.json.
+
+One step = one full run of that workload (epi_engine_run: all hours, interventions and the
+stop rule), restarted from the same initial world (a device-side restore) each step.
+  value  agent-hours/s with the world resident in HBM, CUDA events on the engine's stream
+  e2e    the same through the C ABI from host buffers: create from host records (upload),
+         run, hourly counts back to the host, destroy -- every step
+The L2 (129 MB) is flushed between steps by writing a 512 MiB buffer; within a step the
+1M-agent working set (~60 MB) is L2-resident by design.
+
+--impl reference times the CPU port of the reference's own tick data flow (hash map,
+threaded map phase, serial resolve; oracle/o2.c) on all host cores.  Under torchrun the
+engine runs as independent replicas (one per GPU, different seeds): the tick has no
+exchange step to shard.
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import os
+import statistics
+import subprocess
+import sys
+import threading
+import time
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+DEFAULT_CONFIG = os.path.join(ROOT, "tests", "golden", "c2_small_pox_1m.json")
+METRIC = "agent-hours/s"
+# Algorithmic bytes of one k_decide launch per agent: pos 4 + st 8 + home 4 + work 4 read,
+# st 8 + tgt 4 written; plus one read of the (G+1)^2 byte occupancy plane.
+DECIDE_BYTES_PER_AGENT = 32
+
+
+def _peaks():
+    try:
+        with open(os.path.join(ROOT, "MEASURED_PEAKS.json")) as f:
+            p = json.load(f)
+        return float(p["hbm_gbs"]), "measured"
+    except Exception:
+        return 6800.0, "fallback"
+
+
+class ClockSampler:
+    """nvidia-smi sampling of SM clocks and throttle reasons during the timed region."""
+
+    FIELDS = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+              "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+              "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, gpu_index: int):
+        self.gpu = gpu_index
+        self.proc = None
+        self.lines: list[str] = []
+        self.thread = None
+
+    def start(self):
+        try:
+            self.proc = subprocess.Popen(
+                ["nvidia-smi", f"--id={self.gpu}", f"--query-gpu={self.FIELDS}", "--format=csv,noheader,nounits",
+                 "-lms", "200"], stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+        except (FileNotFoundError, OSError):
+            self.proc = None
+            return
+        self.thread = threading.Thread(target=self._read, daemon=True)
+        self.thread.start()
+
+    def _read(self):
+        for line in self.proc.stdout:
+            self.lines.append(line.strip())
+
+    def stop(self) -> dict:
+        if self.proc is None:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["nvidia-smi unavailable"]}
+        self.proc.terminate()
+        try:
+            self.proc.wait(timeout=5)
+        except subprocess.TimeoutExpired:
+            self.proc.kill()
+        if self.thread:
+            self.thread.join(timeout=2)
+        sm, smax, reasons = [], [], set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for line in self.lines:
+            parts = [p.strip() for p in line.split(",")]
+            if len(parts) < 9:
+                continue
+            try:
+                sm.append(float(parts[1]))
+                smax.append(float(parts[2]))
+            except ValueError:
+                continue
+            for name, v in zip(names, parts[5:9]):
+                if v.lower() == "active":
+                    reasons.add(name)
+        return {"sm_mhz": statistics.median(sm) if sm else None, "sm_max_mhz": max(smax) if smax else None,
+                "reasons": sorted(reasons), "samples": len(sm)}
+
+
+def _dist():
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    return world, rank, local
+
+
+def _agent_hours(rows, n_agents: int) -> float:
+    return float(n_agents) * float(len(rows))
+
+
+def cpu_baseline(cfg: dict, records, seconds: float = 12.0, max_hours: int = 240) -> dict:
+    """O2 (the reference-semantics port) on all host cores over the first hours of the run."""
+    import numpy as np  # noqa: F401
+
+    from oracle import oracle
+
+    threads = os.cpu_count() or 1
+    params = oracle.params_from_config(cfg)
+    sim = oracle.O2(params, records, threads=threads)
+    t0 = time.perf_counter()
+    hours = 0
+    while hours < max_hours and (time.perf_counter() - t0) < seconds:
+        sim.run(1 + hours, 2 + hours, interventions=True, stop=False, keep_rows=False)
+        hours += 1
+    dt = time.perf_counter() - t0
+    n = len(records)
+    return {"value": n * hours / dt, "unit": METRIC, "cores": threads, "kind": "port",
+            "sample": f"oracle/o2.c (reference data flow: FNV hash map, threaded map phase, serial "
+                      f"resolve) on the same {n}-agent world, hours 1..{hours} ({dt:.1f} s)"}
+
+
+def run_reference(args, cfg):
+    world, rank, _ = _dist()
+    if rank != 0:
+        return
+    from epirust_gb300 import Config
+    from epirust_gb300.engine import world_build
+    from oracle import oracle
+
+    records, _ = world_build(Config(json.dumps(cfg)).params)
+    threads = os.cpu_count() or 1
+    params = oracle.params_from_config(cfg)
+    n = len(records)
+    sample_hours = args.ref_hours
+
+    def step():
+        sim = oracle.O2(params, records, threads=threads)
+        t0 = time.perf_counter()
+        sim.run(1, 1 + sample_hours, interventions=True, stop=False, keep_rows=False)
+        return time.perf_counter() - t0
+
+    for _ in range(args.warmup):
+        step()
+    times = [step() for _ in range(args.steps)]
+    total = sum(times)
+    value = n * sample_hours * args.steps / total
+    line = {
+        "impl": "reference", "metric": METRIC, "value": value, "unit": METRIC, "n_gpus": world, "steps": args.steps,
+        "warmup": args.warmup, "ms_per_step": 1000 * total / args.steps, "higher_is_better": True,
+        "scaling": "weak", "vs_baseline": None, "dtype": "u32", "data": "synthetic",
+        "config": {"workload": "plain single-engine tick, 1M agents, 2500 grid (first "
+                               f"{sample_hours} h of the 4800 h run per step)", "parallelism": "cpu threads",
+                   "threads": threads},
+        "cpu_baseline": {"value": value, "unit": METRIC, "cores": threads, "kind": "port",
+                         "sample": f"hours 1..{sample_hours} of the {n}-agent world per step"},
+        "e2e": {"value": value, "unit": METRIC, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+    }
+    print(json.dumps(line), flush=True)
+
+
+def run_gpu(args, cfg):
+    import numpy as np
+    import torch
+
+    from epirust_gb300 import AGENT_DTYPE, Config, Epidemiology, build
+    from epirust_gb300.engine import world_build
+
+    build.build()
+    world, rank, local = _dist()
+    if world > 1:
+        import torch.distributed as dist
+
+        dist.init_process_group("nccl" if torch.cuda.is_available() else "gloo")
+    torch.cuda.set_device(local)
+    dev_index = torch.cuda.current_device()
+    cfg = dict(cfg)
+    cfg["seed"] = int(cfg.get("seed", 0)) + 1000 * rank  # independent replicas
+    config = Config(json.dumps(cfg))
+    n = config.number_of_agents
+    G = config.params.grid_size
+    cells = (G + 1) ** 2
+    records, _ = world_build(config.params)
+
+    stream = torch.cuda.Stream()
+    flush = torch.empty(512 << 20, dtype=torch.uint8, device="cuda")
+
+    eng = Epidemiology(config, records=records)
+    eng.set_stream(stream.cuda_stream)
+    eng.save_state()
+
+    def step():
+        eng.restore_state()
+        return eng.run()
+
+    for _ in range(args.warmup):
+        with torch.cuda.stream(stream):
+            flush.fill_(1)
+        step()
+    torch.cuda.synchronize()
+
+    def barrier():
+        if world > 1:
+            import torch.distributed as dist
+
+            dist.barrier()
+        torch.cuda.synchronize()
+
+    # ---- timed region: device-resident world
+    sampler = ClockSampler(dev_index)
+    sampler.start()
+    launches0 = eng.kernels_launched()
+    barrier()
+    ms_total, agent_hours = 0.0, 0.0
+    t_wall = time.perf_counter()
+    for k in range(args.steps):
+        with torch.cuda.stream(stream):
+            flush.fill_(k & 0xFF)
+        ev0, ev1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        ev0.record(stream)
+        rows = step()
+        ev1.record(stream)
+        ev1.synchronize()
+        ms_total += ev0.elapsed_time(ev1)
+        agent_hours += _agent_hours(rows, n)
+    barrier()
+    wall = time.perf_counter() - t_wall
+    clocks = sampler.stop()
+    launches = eng.kernels_launched() - launches0
+    hours_per_step = len(rows)
+
+    if world > 1:
+        import torch.distributed as dist
+
+        t = torch.tensor([ms_total, agent_hours], dtype=torch.float64, device="cuda")
+        ms_max = t[0].clone()
+        dist.all_reduce(ms_max, op=dist.ReduceOp.MAX)
+        dist.all_reduce(t[1:], op=dist.ReduceOp.SUM)
+        ms_total, agent_hours = float(ms_max), float(t[1])
+    value = agent_hours / (ms_total / 1000.0)
+
+    # ---- e2e: host records -> create (upload) -> run -> counts on the host -> destroy
+    pinned = torch.from_numpy(records.view(np.uint8)).pin_memory()
+    host_records = pinned.numpy().view(AGENT_DTYPE)
+    e2e_steps = max(1, min(args.steps, 3))
+    e2e_ms, e2e_ah = 0.0, 0.0
+    for _ in range(e2e_steps):
+        with torch.cuda.stream(stream):
+            flush.fill_(3)
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        e = Epidemiology(config, records=host_records)
+        r = e.run()
+        e.close()
+        e2e_ms += 1000.0 * (time.perf_counter() - t0)
+        e2e_ah += _agent_hours(r, n)
+    e2e_value = e2e_ah / (e2e_ms / 1000.0)
+
+    # ---- roofline of the dominant kernel: CUDA events around every launch (no graphs)
+    prof = Epidemiology(config, records=records)
+    prof.set_stream(stream.cuda_stream)
+    prof.set_profiling(True)
+    prof.simulate_hours(1, 72)
+    stats = prof.kernel_stats()
+    prof.close()
+    total_kernel_ms = sum(ms for _, ms in stats.values())
+    launches_d, ms_d = stats["k_decide"]
+    avg_ms = ms_d / max(launches_d, 1)
+    alg_bytes = DECIDE_BYTES_PER_AGENT * n + cells
+    achieved = alg_bytes / (avg_ms / 1000.0) / 1e9
+    peak, peak_kind = _peaks()
+    traffic = None
+    tpath = os.path.join(ROOT, "profiles", "k_decide_traffic.json")
+    if os.path.exists(tpath):
+        with open(tpath) as f:
+            traffic = json.load(f).get("bytes_per_launch")
+
+    cpu = cpu_baseline(cfg, records, seconds=args.cpu_seconds) if rank == 0 and not args.no_cpu else None
+
+    if rank == 0:
+        line = {
+            "metric": METRIC, "value": value, "unit": METRIC, "n_gpus": world, "steps": args.steps,
+            "warmup": args.warmup, "ms_per_step": ms_total / args.steps, "higher_is_better": True,
+            "scaling": "weak", "vs_baseline": None, "dtype": "u32", "data": "synthetic",
+            "config": {"workload": "plain single-engine tick: 1M agents, 2500 grid, 4800 h, lockdown + "
+                                   "vaccination + hospital build (tests/golden/c2_small_pox_1m.json)",
+                       "agents": n, "grid": G, "hours_per_step": hours_per_step, "parallelism": f"replicas{world}",
+                       "l2": "flushed between steps (512 MiB write); inputs L2-resident within a step",
+                       "wall_s": wall},
+            "roofline": {"bound": "hbm", "kernel": "k_decide", "achieved": achieved, "peak": peak, "unit": "GB/s",
+                         "frac": achieved / peak, "peak_kind": peak_kind, "traffic": traffic,
+                         "alg_bytes_per_launch": alg_bytes, "avg_launch_ms": avg_ms,
+                         "share_of_kernel_time": ms_d / total_kernel_ms if total_kernel_ms else None,
+                         "kernels": {k: {"launches": v[0], "ms": v[1]} for k, v in stats.items() if v[0]}},
+            "cpu_baseline": cpu,
+            "e2e": {"value": e2e_value, "unit": METRIC, "h2d_bytes_per_step": int(n * 24),
+                    "d2h_bytes_per_step": int(hours_per_step * 32), "steps": e2e_steps},
+            "gpu_launches": int(launches),
+            "clocks": clocks,
+        }
+        print(json.dumps(line), flush=True)
+    if world > 1:
+        import torch.distributed as dist
+
+        dist.destroy_process_group()
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=5)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
+    ap.add_argument("--config", default=DEFAULT_CONFIG)
+    ap.add_argument("--cpu-seconds", type=float, default=12.0)
+    ap.add_argument("--ref-hours", type=int, default=24)
+    ap.add_argument("--no-cpu", action="store_true")
+    args = ap.parse_args()
+    with open(args.config) as f:
+        cfg = json.load(f)
+    if args.impl == "reference":
+        run_reference(args, cfg)
+    else:
+        run_gpu(args, cfg)
+
+
+if __name__ == "__main__":
+    main()

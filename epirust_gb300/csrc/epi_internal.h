@@ -1,0 +1,138 @@
+// epi_internal.h -- layouts shared by the host world builder and the sm_103a kernels.
+//
+// Agent state lives on the device as struct-of-arrays of packed 32-bit words:
+//   pos[i]   x | y << 16                     (x, y in [0, G]; 15 bits each)
+//   st[i].x  disease state, flags, current-area code, work status, immunity, infection day
+//   st[i].y  at_hour of Exposed / Infected-Pre
+//   home[i]  start corner of the 2x2 house  (packed like pos)
+//   work[i]  start corner of the 10x10 office (packed like pos; the house for non-workers)
+//   wsa[i]   work_start_at of hospital staff (read only for staff)
+// The occupancy plane is one byte per cell of the (G+1) x (G+1) plane (the reference's
+// areas reach row and column G, engine/src/geography/mod.rs:42-48):
+//   0 = vacant, 1 = occupied and not infectious, 2 = infectious at the regular rate,
+//   3 = infectious at the high rate.
+// A u32 claim plane of the same extent resolves cell conflicts (lowest agent index wins).
+#pragma once
+
+#include <stdint.h>
+
+#include "../../include/epi_engine.h"
+
+#if defined(__CUDACC__)
+#define EPI_HD __host__ __device__ __forceinline__
+#else
+#define EPI_HD inline
+#endif
+
+namespace epi {
+
+// ---- st.x bit fields
+constexpr uint32_t kStateMask = 0x7u;
+constexpr uint32_t kHosp = 1u << 3;
+constexpr uint32_t kIso = 1u << 4;
+constexpr uint32_t kVacc = 1u << 5;
+constexpr uint32_t kWq = 1u << 6;
+constexpr uint32_t kPt = 1u << 7;
+constexpr int kAreaShift = 8;  // 3 bits
+constexpr int kWsShift = 11;   // 2 bits
+constexpr int kImmShift = 13;  // 3 bits, immunity + 2
+constexpr int kDayShift = 16;  // 16 bits
+constexpr uint32_t kAreaMask = 0x7u << kAreaShift;
+constexpr uint32_t kWsMask = 0x3u << kWsShift;
+constexpr uint32_t kDayMask = 0xFFFFu << kDayShift;
+
+// current_area codes; HOME/WORK decode through the agent's home/work corner
+enum AreaCode : uint32_t { kHome = 0, kWork = 1, kTransport = 2, kHousing = 3, kHosp0 = 4, kHosp1 = 5, kNumAreas = 6 };
+
+constexpr uint32_t kNoAction = 0xFFFFFFFFu;  // tgt[i]: nothing to commit
+constexpr uint32_t kNoClaim = 0xFFFFFFFFu;   // claim plane: free
+constexpr uint32_t kWorldHour = 0xFFFFFFFFu; // Philox counter word 1 of world-build draws
+constexpr uint32_t kMaxHours = 1500000u;     // infection day fits 16 bits
+
+EPI_HD uint32_t st_state(uint32_t s) { return s & kStateMask; }
+EPI_HD uint32_t st_area(uint32_t s) { return (s >> kAreaShift) & 7u; }
+EPI_HD uint32_t st_ws(uint32_t s) { return (s >> kWsShift) & 3u; }
+EPI_HD int32_t st_imm(uint32_t s) { return (int32_t)((s >> kImmShift) & 7u) - 2; }
+EPI_HD uint32_t st_day(uint32_t s) { return s >> kDayShift; }
+EPI_HD uint32_t with_area(uint32_t s, uint32_t a) { return (s & ~kAreaMask) | (a << kAreaShift); }
+EPI_HD uint32_t with_ws(uint32_t s, uint32_t w) { return (s & ~kWsMask) | (w << kWsShift); }
+EPI_HD uint32_t with_state(uint32_t s, uint32_t v) { return (s & ~kStateMask) | v; }
+EPI_HD uint32_t with_day(uint32_t s, uint32_t d) { return (s & ~kDayMask) | (d << kDayShift); }
+EPI_HD bool infected(uint32_t s) { uint32_t v = s & kStateMask; return v >= EPI_I_PRE && v <= EPI_I_SEVERE; }
+
+EPI_HD uint32_t pack_xy(int32_t x, int32_t y) { return (uint32_t)x | ((uint32_t)y << 16); }
+EPI_HD int32_t unpack_x(uint32_t p) { return (int32_t)(p & 0x7FFFu); }
+EPI_HD int32_t unpack_y(uint32_t p) { return (int32_t)((p >> 16) & 0x7FFFu); }
+
+struct Rect { int32_t x0, y0, x1, y1; };
+
+EPI_HD bool rect_has(const Rect& r, int32_t x, int32_t y) { return r.x0 <= x && x <= r.x1 && r.y0 <= y && y <= r.y1; }
+EPI_HD bool rect_eq(const Rect& a, const Rect& b) { return a.x0 == b.x0 && a.y0 == b.y0 && a.x1 == b.x1 && a.y1 == b.y1; }
+
+// Per-engine constants, in device global memory (read through a const __restrict__ pointer).
+struct DevParams {
+    uint32_t n;                 // agents
+    int32_t G;                  // grid size
+    int32_t W;                  // plane width G + 1
+    uint32_t hosp_code;         // kHosp0 or kHosp1: the current hospital_area
+    Rect area[kNumAreas];       // global areas by code (HOME/WORK slots unused)
+    uint32_t key0, key1;        // Philox key = seed
+    uint32_t reg_start, high_start, last_day;
+    uint32_t exposed_duration, pre_duration;
+    uint32_t hosp_if_class;     // bit c: rate of class c >= high rate (c = 0 none, 1 reg, 2 high)
+    uint64_t thr_rate[3];       // Bernoulli thresholds of the rate classes
+    uint64_t thr_death, thr_symptoms, thr_severe;
+};
+
+// Bernoulli(p) as a threshold on a uniform 32-bit word: gen_bool(p) <=> u < thr.
+inline uint64_t bernoulli_threshold(double p) {
+    if (!(p > 0.0)) return 0ull;
+    if (p >= 1.0) return 1ull << 32;
+    return (uint64_t)(p * 4294967296.0);
+}
+
+// Uniform index in [0, k) from one 32-bit word (multiply-high).
+EPI_HD uint32_t uniform_index(uint32_t u, uint32_t k) { return (uint32_t)(((uint64_t)u * (uint64_t)k) >> 32); }
+
+// Rate class of get_current_transmission_rate(day), common/src/disease/mod.rs:88-95.
+EPI_HD uint32_t rate_class(uint32_t reg_start, uint32_t high_start, uint32_t last_day, uint32_t day) {
+    if (reg_start < day && day <= high_start) return 1u;
+    if (high_start < day && day <= last_day) return 2u;
+    return 0u;
+}
+
+// Philox4x32-10 (Salmon et al., SC'11): ten rounds of two 32x32->64 multiplies whose
+// halves are crossed with the odd counter words and the round key; key += Weyl constants.
+EPI_HD void philox4x32(uint32_t c0, uint32_t c1, uint32_t c2, uint32_t c3, uint32_t k0, uint32_t k1,
+                       uint32_t out[4]) {
+    for (int r = 0; r < 10; ++r) {
+#if defined(__CUDA_ARCH__)
+        uint32_t hi_a = __umulhi(0xD2511F53u, c0), lo_a = 0xD2511F53u * c0;
+        uint32_t hi_b = __umulhi(0xCD9E8D57u, c2), lo_b = 0xCD9E8D57u * c2;
+#else
+        uint64_t pa = 0xD2511F53ull * c0, pb = 0xCD9E8D57ull * c2;
+        uint32_t hi_a = (uint32_t)(pa >> 32), lo_a = (uint32_t)pa;
+        uint32_t hi_b = (uint32_t)(pb >> 32), lo_b = (uint32_t)pb;
+#endif
+        uint32_t t0 = hi_b ^ c1 ^ k0;
+        uint32_t t2 = hi_a ^ c3 ^ k1;
+        c0 = t0; c1 = lo_b; c2 = t2; c3 = lo_a;
+        k0 += 0x9E3779B9u;
+        k1 += 0xBB67AE85u;
+    }
+    out[0] = c0; out[1] = c1; out[2] = c2; out[3] = c3;
+}
+
+// Draw-block ids of the counter word 2 (the layout every consumer of the streams shares).
+enum DrawBlock : uint32_t {
+    kBlkMove = 0,     // u0,u1 random point; u2 Moore choice (movement) / death (hour 23)
+    kBlkDisease = 1,  // Susceptible neighbours 0-3 | Exposed jitter, symptoms | Pre severe
+    kBlkDisease2 = 2, // Susceptible neighbours 4-7
+    kBlkVaccine = 3,
+    kBlkCitizen = 16, // world build: working, public transport, hospital staff, immunity
+    kBlkEssential = 17,
+    kBlkHouse = 18,   // counter word 0 = house index
+    kBlkInfectPick = 19
+};
+
+}  // namespace epi

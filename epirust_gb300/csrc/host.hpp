@@ -1,0 +1,63 @@
+// host.hpp -- host-side pieces of the engine: config, geography, world build, the
+// intervention triggers and the output listeners.  No CUDA in here.
+#pragma once
+
+#include <string>
+#include <vector>
+
+#include "epi_internal.h"
+
+namespace epi {
+
+// Config::read equivalent; throws std::runtime_error with a message on bad input.
+epi_params params_from_json(const std::string& text);
+// Range checks the engine needs (percentages in [0,1], sizes, hours); "" when fine.
+std::string validate_params(const epi_params& p);
+
+epi_geography define_geography(uint32_t grid_size);
+void resize_hospital(epi_geography& g, int32_t number_of_agents, double staff_pct, double beds_pct);
+epi_area grown_hospital(const epi_geography& initial);
+
+epi_area house_area(const epi_geography& g, uint32_t k);
+epi_area office_area(const epi_geography& g, uint32_t k);
+
+// Epidemiology::new world build on the host (geography, population, starting infections,
+// start points, hospital resize, essential workers).  Returns EPI_OK or an error code.
+int build_world(const epi_params& p, std::vector<epi_agent_record>& out, epi_geography& geo, std::string& err);
+
+struct Report {
+    uint32_t hour;
+    std::string name, data;
+};
+
+// State of LockdownIntervention / BuildNewHospital / VaccinateIntervention between hours.
+struct InterventionState {
+    bool locked = false;
+    uint32_t zero_infection_hour = 0;
+    uint32_t new_infections_in_a_day = 0;
+    bool hospital_applied = false;
+    std::vector<Report> reports;
+};
+
+struct InterventionActions {
+    bool vaccinate = false;
+    double vaccinate_percent = 0.0;
+    bool lock = false, unlock = false, grow_hospital = false;
+    uint32_t applied = 0;  // EPI_IV_* bits
+};
+
+// Trigger logic of process_interventions for this hour's counts (updates st and
+// st.reports); the caller applies the returned bulk actions to the agents in the order
+// vaccinate, lock, unlock, grow (allocation_map.rs:315-336).
+InterventionActions decide_interventions(const epi_params& p, InterventionState& st, const epi_counts& c,
+                                         const epi_area& hospital);
+
+// Is this hour one at which an intervention can fire (a day boundary or a vaccination
+// hour)?  Hour segments of the run loop end at these hours.
+bool is_event_hour(const epi_params& p, uint32_t hour);
+
+// CsvListener + InterventionReporter output files.
+int write_outputs(const std::string& dir, const std::string& engine_id, const std::vector<epi_counts>& rows,
+                  const std::vector<Report>& reports, std::string& err);
+
+}  // namespace epi

@@ -1,0 +1,290 @@
+// tick.cuh -- the per-agent hourly rules as sm_103a device code.
+//
+// One thread owns one agent for one hour.  It reads the agent's packed words and the
+// previous-hour occupancy plane (never another agent's record), proposes a target cell,
+// updates its own disease state, and claims the target with atomicMin on the claim plane.
+// The rules follow engine/src/citizen/mod.rs:215-454,
+// engine/src/state_machine/default_disease_handler.rs:31-103 and
+// engine/src/allocation_map.rs:136-163; random draws are fixed words of per-agent-hour
+// Philox blocks (counter = agent, hour, block, 0).
+#pragma once
+
+#include "epi_internal.h"
+
+namespace epi {
+
+// Moore offsets in NeighborIterator order (engine/src/geography/point.rs:59), packed as
+// 2-bit (d + 1) fields: k-th neighbour = (x + dx(k), y + dy(k)).
+__device__ __forceinline__ int32_t nb_dx(int k) { return (int32_t)((0x9224u >> (2 * k)) & 3u) - 1; }
+__device__ __forceinline__ int32_t nb_dy(int k) { return (int32_t)((0xA940u >> (2 * k)) & 3u) - 1; }
+
+struct PlaneView {
+    const uint8_t* __restrict__ cells;
+    int32_t G, W;
+    int* err;
+    // The only cells a rule can address lie in [0, G]^2 by construction; anything else is
+    // reported through err and treated as occupied instead of being dereferenced.
+    __device__ __forceinline__ uint32_t at(int32_t x, int32_t y) const {
+        if ((uint32_t)x > (uint32_t)G || (uint32_t)y > (uint32_t)G) {
+            atomicOr(err, 1);
+            return 1u;
+        }
+        return __ldg(cells + (size_t)y * (size_t)W + (size_t)x);
+    }
+    __device__ __forceinline__ bool vacant(int32_t x, int32_t y) const { return at(x, y) == 0u; }
+    __device__ __forceinline__ bool in_grid(int32_t x, int32_t y) const {
+        return x >= 0 && y >= 0 && x < G && y < G;  // is_point_in_grid, allocation_map.rs:156-159
+    }
+};
+
+// Lazily materialised Philox blocks of one agent-hour.
+struct Draws {
+    uint32_t agent, hour, k0, k1;
+    uint32_t have = 0;
+    uint32_t b0[4], b1[4], b2[4];
+    __device__ __forceinline__ uint32_t m(int w) {
+        if (!(have & 1u)) { philox4x32(agent, hour, kBlkMove, 0u, k0, k1, b0); have |= 1u; }
+        return b0[w];
+    }
+    __device__ __forceinline__ uint32_t d(int w) {
+        if (!(have & 2u)) { philox4x32(agent, hour, kBlkDisease, 0u, k0, k1, b1); have |= 2u; }
+        return b1[w];
+    }
+    __device__ __forceinline__ uint32_t d2(int w) {
+        if (!(have & 4u)) { philox4x32(agent, hour, kBlkDisease2, 0u, k0, k1, b2); have |= 4u; }
+        return b2[w];
+    }
+};
+
+struct Cell { int32_t x, y; };
+
+__device__ __forceinline__ Cell random_point(const Rect& a, uint32_t ux, uint32_t uy) {
+    Cell c;
+    c.x = a.x0 + (int32_t)uniform_index(ux, (uint32_t)(a.x1 - a.x0 + 1));
+    c.y = a.y0 + (int32_t)uniform_index(uy, (uint32_t)(a.y1 - a.y0 + 1));
+    return c;
+}
+
+__device__ __forceinline__ Rect home_rect(uint32_t home) {
+    int32_t x = unpack_x(home), y = unpack_y(home);
+    return Rect{x, y, x + 1, y + 1};
+}
+__device__ __forceinline__ Rect office_rect(uint32_t work) {
+    int32_t x = unpack_x(work), y = unpack_y(work);
+    return Rect{x, y, x + 9, y + 9};
+}
+__device__ __forceinline__ Rect area_rect(const DevParams& P, uint32_t code, uint32_t home, uint32_t work) {
+    if (code == kHome) return home_rect(home);
+    if (code == kWork) return office_rect(work);
+    return P.area[code];
+}
+
+// Citizen::can_move, citizen/mod.rs:452-454
+__device__ __forceinline__ bool can_move(uint32_t s) {
+    uint32_t v = s & kStateMask;
+    return !(v == EPI_I_MILD || v == EPI_I_SEVERE || v == EPI_D || (s & (kHosp | kIso)));
+}
+
+// Plane byte of an occupied cell: 1 + transmission-rate class of an infectious occupant.
+__device__ __forceinline__ uint32_t cell_class(const DevParams& P, uint32_t s) {
+    if (!infected(s) || (s & kHosp)) return 1u;
+    uint32_t d = (uint32_t)((int32_t)st_day(s) + st_imm(s));  // (day as i32 + immunity) as Day
+    return 1u + rate_class(P.reg_start, P.high_start, P.last_day, d);
+}
+
+// Citizen::move_agent_from, citizen/mod.rs:415-432
+__device__ __forceinline__ Cell move_agent_from(const PlaneView& pl, uint32_t s, const Rect& cur, Cell cell, Draws& dr) {
+    if (!can_move(s)) return cell;
+    Cell c = cell;
+    if (!rect_has(cur, cell.x, cell.y)) c = random_point(cur, dr.m(0), dr.m(1));
+    uint32_t mask = 0;
+#pragma unroll
+    for (int k = 0; k < 8; ++k) {
+        int32_t qx = c.x + nb_dx(k), qy = c.y + nb_dy(k);
+        if (rect_has(cur, qx, qy) && pl.in_grid(qx, qy) && pl.vacant(qx, qy)) mask |= 1u << k;
+    }
+    if (!mask) return cell;
+    uint32_t j = uniform_index(dr.m(2), (uint32_t)__popc(mask));
+    // position of the j-th set bit
+    uint32_t m = mask;
+#pragma unroll
+    for (int t = 0; t < 7; ++t)
+        if (t < (int)j) m &= m - 1u;
+    int k = __ffs(m) - 1;
+    return Cell{c.x + nb_dx(k), c.y + nb_dy(k)};  // vacant by construction: move_agent keeps it
+}
+
+// Citizen::goto_area, citizen/mod.rs:367-395
+__device__ __forceinline__ Cell goto_area(const PlaneView& pl, uint32_t s, const Rect& cur, const Rect& target,
+                                          uint32_t home, uint32_t work, Cell cell, Draws& dr) {
+    const uint32_t ws = st_ws(s), v = s & kStateMask;
+    bool override_movement = false;
+    if (ws == EPI_WS_NORMAL || ws == EPI_WS_ESSENTIAL) {
+        if (rect_has(office_rect(work), cell.x, cell.y) && rect_eq(target, home_rect(home)) &&
+            (v == EPI_I_MILD || v == EPI_I_SEVERE))
+            override_movement = true;
+    }
+    if (!can_move(s) && !override_movement) return cell;
+    if (ws != EPI_WS_NA) {
+        Cell q = random_point(target, dr.m(0), dr.m(1));
+        return pl.vacant(q.x, q.y) ? q : cell;
+    }
+    return move_agent_from(pl, s, cur, cell, dr);
+}
+
+// DiseaseStateMachine::next with the default DiseaseHandler (ddh:41-86) for the hour's
+// proposed cell; at is the Exposed/Pre at_hour word.
+__device__ __forceinline__ void infection_dynamics(const DevParams& P, const PlaneView& pl, uint32_t& s, uint32_t& at,
+                                                   const Rect& cur, Cell cell, uint32_t hour, Draws& dr) {
+    const uint32_t v = s & kStateMask;
+    if (v == EPI_S) {
+        if (s & (kWq | kVacc)) return;
+#pragma unroll
+        for (int k = 0; k < 8; ++k) {
+            int32_t qx = cell.x + nb_dx(k), qy = cell.y + nb_dy(k);
+            if (!rect_has(cur, qx, qy) || !pl.in_grid(qx, qy)) continue;
+            uint32_t b = pl.at(qx, qy);
+            if (b < 2u) continue;
+            uint32_t u = k < 4 ? dr.d(k) : dr.d2(k - 4);
+            if ((uint64_t)u < P.thr_rate[b - 1u]) {
+                s = with_state(s, EPI_E);
+                at = hour;
+                return;
+            }
+        }
+    } else if (v == EPI_E) {
+        int32_t jitter = (int32_t)uniform_index(dr.d(0), 3u) - 1;
+        uint32_t need = (uint32_t)((int32_t)P.exposed_duration + jitter);
+        if (hour - at >= need) {
+            bool symptoms = (uint64_t)dr.d(1) < P.thr_symptoms;
+            s = with_day(s, 0u);
+            if (symptoms) { s = with_state(s, EPI_I_PRE); at = hour; }
+            else s = with_state(s, EPI_I_ASYM);
+        }
+    } else if (v == EPI_I_PRE) {
+        if (hour - at >= P.pre_duration)
+            s = with_state(s, (uint64_t)dr.d(0) < P.thr_severe ? EPI_I_SEVERE : EPI_I_MILD);
+    }
+}
+
+// Citizen::perform_movements, citizen/mod.rs:257-349 (hours 7..22 of the day).
+__device__ __forceinline__ Cell perform_movements(const DevParams& P, const PlaneView& pl, uint32_t& s, uint32_t& at,
+                                                  uint32_t& wsa, uint32_t home, uint32_t work, Cell cell,
+                                                  uint32_t hod, uint32_t hour, Draws& dr) {
+    const uint32_t ws = st_ws(s);
+    Cell nc = cell;
+    Rect cur = area_rect(P, st_area(s), home, work);
+    if (ws == EPI_WS_NORMAL || ws == EPI_WS_ESSENTIAL) {
+        if (hod == 7u || hod == 17u) {
+            if (s & kPt) {
+                nc = goto_area(pl, s, cur, P.area[kTransport], home, work, cell, dr);
+                s = with_area(s, kTransport);
+            } else {
+                nc = move_agent_from(pl, s, cur, cell, dr);
+            }
+        } else if (hod == 8u) {
+            nc = goto_area(pl, s, cur, office_rect(work), home, work, cell, dr);
+            s = with_area(s, kWork);
+        } else if (hod == 16u) {
+            nc = goto_area(pl, s, cur, home_rect(home), home, work, cell, dr);
+            s = with_area(s, kHome);
+        } else {
+            nc = move_agent_from(pl, s, cur, cell, dr);
+        }
+    } else if (ws == EPI_WS_HOSPITAL_STAFF) {
+        const uint32_t since = hour >= wsa ? hour - wsa : 0u;  // saturating_sub
+        if (since == 24u * 14u) {
+            s |= kWq;
+            return nc;
+        }
+        if (since == 24u * 14u * 2u) {
+            nc = goto_area(pl, s, cur, home_rect(home), home, work, cell, dr);
+            s = with_area(s, kHome);
+            wsa = hour + 24u * 14u;
+            return nc;
+        }
+        if (hod == 8u) {
+            const Rect hosp = P.area[P.hosp_code];
+            if (!rect_eq(cur, hosp) && wsa <= hour) {
+                nc = goto_area(pl, s, cur, hosp, home, work, cell, dr);
+                s = with_area(s, P.hosp_code);
+                wsa = hour;
+            }
+            s &= ~kWq;
+        } else if (hod == 16u) {
+            s |= kWq;
+        } else if (!(s & kWq) && can_move(s)) {
+            nc = move_agent_from(pl, s, cur, cell, dr);
+        }
+    } else {  // NA
+        if (hod == 8u) {
+            nc = goto_area(pl, s, cur, P.area[kHousing], home, work, cell, dr);
+            s = with_area(s, kHousing);
+        } else if (hod == 12u) {
+            nc = goto_area(pl, s, cur, home_rect(home), home, work, cell, dr);
+            s = with_area(s, kHome);
+        } else {
+            nc = move_agent_from(pl, s, cur, cell, dr);
+        }
+    }
+    infection_dynamics(P, pl, s, at, area_rect(P, st_area(s), home, work), nc, hour, dr);
+    return nc;
+}
+
+// Hour 0 of the day: increment_infection_day, then Citizen::hospitalize
+// (citizen/mod.rs:240-243, 351-365; allocation_map.rs:144-150).  hosp_first is the first
+// vacant hospital cell of the snapshot in area-iterator order (packed) or kNoAction.
+__device__ __forceinline__ bool wants_hospital(const DevParams& P, uint32_t s) {
+    if ((s & kHosp) || (s & kStateMask) != EPI_I_SEVERE) return false;
+    uint32_t d = (uint32_t)((int32_t)st_day(s) + st_imm(s));
+    return (P.hosp_if_class >> rate_class(P.reg_start, P.high_start, P.last_day, d)) & 1u;
+}
+
+__device__ __forceinline__ Cell routine_start(const DevParams& P, const PlaneView& pl, uint32_t& s, uint32_t home,
+                                              Cell cell, uint32_t hosp_first, Draws& dr) {
+    if (infected(s)) s = with_day(s, st_day(s) + 1u);
+    if (!wants_hospital(P, s)) return cell;
+    if (hosp_first != kNoAction) {
+        s |= kHosp;
+        return Cell{unpack_x(hosp_first), unpack_y(hosp_first)};
+    }
+    Cell q = random_point(home_rect(home), dr.m(0), dr.m(1));
+    return pl.vacant(q.x, q.y) ? q : cell;
+}
+
+// Hour 23: Citizen::deceased with on_routine_end (citizen/mod.rs:397-413, ddh:88-102).
+__device__ __forceinline__ Cell routine_end(const DevParams& P, const PlaneView& pl, uint32_t& s, uint32_t home,
+                                            Cell cell, Draws& dr) {
+    const uint32_t v = s & kStateMask, day = st_day(s);
+    if (v == EPI_I_ASYM && day == 9u) s = with_state(s, EPI_R);          // ASYMPTOMATIC_LAST_DAY
+    else if (v == EPI_I_MILD && day == 12u) s = with_state(s, EPI_R);    // MILD_INFECTED_LAST_DAY
+    else if (v == EPI_I_SEVERE && day == P.last_day)
+        s = with_state(s, (uint64_t)dr.m(2) < P.thr_death ? EPI_D : EPI_R);
+    Cell nc = cell;
+    const uint32_t nv = s & kStateMask;
+    if (nv == EPI_R) {
+        Cell q = random_point(home_rect(home), dr.m(0), dr.m(1));
+        if (pl.vacant(q.x, q.y)) nc = q;
+    }
+    if (nv == EPI_R || nv == EPI_D) s &= ~kHosp;
+    return nc;
+}
+
+// Counts::update_counts bin (counts.rs:126-140): 0 S, 1 E, 2 I, 3 H, 4 R, 5 D.
+__device__ __forceinline__ uint32_t count_bin(uint32_t s) {
+    uint32_t v = s & kStateMask;
+    if (v == EPI_S) return 0u;
+    if (v == EPI_E) return 1u;
+    if (v == EPI_R) return 4u;
+    if (v == EPI_D) return 5u;
+    return (s & kHosp) ? 3u : 2u;
+}
+
+// tgt word: target x | y << 16 with the new plane class in bits 15 (low) and 31 (high).
+__device__ __forceinline__ uint32_t encode_target(Cell c, uint32_t cls) {
+    return pack_xy(c.x, c.y) | ((cls & 1u) << 15) | ((cls >> 1) << 31);
+}
+__device__ __forceinline__ uint32_t target_xy(uint32_t t) { return t & 0x7FFF7FFFu; }
+__device__ __forceinline__ uint32_t target_class(uint32_t t) { return ((t >> 15) & 1u) | ((t >> 30) & 2u); }
+
+}  // namespace epi

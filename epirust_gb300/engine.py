@@ -1,0 +1,223 @@
+"""Host side of the engine in the shape of the reference's single-engine API.
+
+    Config.read(path)                 common/src/config/mod.rs:119-123
+    Epidemiology(config, seed)        engine/src/epidemiology_simulation.rs:75-135
+      .run()                          run_single_engine, epidemiology_simulation.rs:211-274
+      .simulate(hour) -> Counts       CitizenLocationMap::simulate, allocation_map.rs:67-129
+      .process_interventions(counts)  allocation_map.rs:306-337
+      .write_outputs(dir)             CsvListener / InterventionReporter
+
+Every call goes through the C ABI of include/epi_engine.h into the CUDA engine.
+"""
+from __future__ import annotations
+
+import ctypes as C
+import json
+from dataclasses import dataclass
+
+import numpy as np
+
+from . import _lib
+from ._lib import AGENT_DTYPE, COUNTS_DTYPE, EpiCounts, EpiGeography, EpiParams, check, lib
+
+
+@dataclass(frozen=True)
+class Counts:
+    """One CSV row (engine/src/models/events/counts.rs:25-34)."""
+    hour: int
+    susceptible: int
+    exposed: int
+    infected: int
+    hospitalized: int
+    recovered: int
+    deceased: int
+
+    @staticmethod
+    def from_c(c: EpiCounts) -> "Counts":
+        return Counts(c.hour, c.susceptible, c.exposed, c.infected, c.hospitalized, c.recovered, c.deceased)
+
+    def to_c(self) -> EpiCounts:
+        return EpiCounts(self.hour, self.susceptible, self.exposed, self.infected, self.hospitalized,
+                         self.recovered, self.deceased)
+
+    def total(self) -> int:
+        return (self.susceptible + self.exposed + self.infected + self.hospitalized + self.recovered
+                + self.deceased)
+
+
+class Config:
+    """The engine's JSON config, parsed by the library (same schema as the reference)."""
+
+    def __init__(self, text: str):
+        self.text = text
+        self.params = EpiParams()
+        err = C.create_string_buffer(512)
+        rc = lib().epi_params_from_json(text.encode(), C.byref(self.params), err, len(err))
+        if rc != _lib.EPI_OK:
+            raise _lib.EpiError(rc, err.value.decode())
+
+    @staticmethod
+    def read(path: str) -> "Config":
+        with open(path) as f:
+            return Config(f.read())
+
+    @staticmethod
+    def from_dict(d: dict) -> "Config":
+        return Config(json.dumps(d))
+
+    @property
+    def hours(self) -> int:
+        return self.params.hours
+
+    @property
+    def number_of_agents(self) -> int:
+        return self.params.number_of_agents
+
+
+def define_geography(grid_size: int) -> EpiGeography:
+    g = EpiGeography()
+    check(lib().epi_define_geography(grid_size, C.byref(g)))
+    return g
+
+
+def world_build(params: EpiParams) -> tuple[np.ndarray, EpiGeography]:
+    """Host world build (population, start points, hospital) as agent records."""
+    n = params.number_of_agents
+    recs = np.zeros(n, dtype=AGENT_DTYPE)
+    g = EpiGeography()
+    check(lib().epi_world_build(C.byref(params), recs.ctypes.data, n, C.byref(g)))
+    return recs, g
+
+
+class Epidemiology:
+    """One single-region engine on the GPU."""
+
+    def __init__(self, config: Config, seed: int | None = None, records: np.ndarray | None = None):
+        self.config = config
+        self.params = EpiParams.from_buffer_copy(config.params)
+        if seed is not None:
+            self.params.seed = seed
+        h = C.c_void_p()
+        if records is None:
+            rc = lib().epi_engine_create(C.byref(self.params), C.byref(h))
+        else:
+            records = np.ascontiguousarray(records, dtype=AGENT_DTYPE)
+            self.params.number_of_agents = len(records)
+            rc = lib().epi_engine_create_from_records(C.byref(self.params), records.ctypes.data, len(records),
+                                                      C.byref(h))
+        check(rc, None)
+        self._h = h
+        self.rows: list[Counts] = []
+
+    # -- lifetime
+    def close(self) -> None:
+        if getattr(self, "_h", None):
+            lib().epi_engine_destroy(self._h)
+            self._h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *exc):
+        self.close()
+
+    @property
+    def handle(self):
+        return self._h
+
+    # -- the tick
+    def simulate(self, hour: int) -> Counts:
+        c = EpiCounts()
+        check(lib().epi_engine_simulate(self._h, hour, C.byref(c)), self._h)
+        return Counts.from_c(c)
+
+    def simulate_hours(self, first_hour: int, n: int) -> np.ndarray:
+        out = np.zeros(n, dtype=COUNTS_DTYPE)
+        check(lib().epi_engine_simulate_hours(self._h, first_hour, n, out.ctypes.data), self._h)
+        return out
+
+    def process_interventions(self, counts: Counts) -> int:
+        applied = C.c_uint32(0)
+        c = counts.to_c()
+        check(lib().epi_engine_process_interventions(self._h, C.byref(c), C.byref(applied)), self._h)
+        return applied.value
+
+    def lock_city(self) -> None:
+        check(lib().epi_engine_lock_city(self._h), self._h)
+
+    def unlock_city(self) -> None:
+        check(lib().epi_engine_unlock_city(self._h), self._h)
+
+    def vaccinate(self, hour: int, percent: float) -> None:
+        check(lib().epi_engine_vaccinate(self._h, hour, percent), self._h)
+
+    def increase_hospital_size(self) -> None:
+        check(lib().epi_engine_increase_hospital_size(self._h), self._h)
+
+    # -- the run loop
+    def run(self) -> np.ndarray:
+        """run_single_engine: hours 1..hours-1 with interventions and the stop rule."""
+        cap = max(self.params.hours, 1)
+        rows = np.zeros(cap, dtype=COUNTS_DTYPE)
+        n = C.c_uint32(0)
+        check(lib().epi_engine_run(self._h, rows.ctypes.data, cap, C.byref(n)), self._h)
+        return rows[: n.value]
+
+    def write_outputs(self, output_dir: str, engine_id: str = "0") -> None:
+        check(lib().epi_engine_write_outputs(self._h, output_dir.encode(), engine_id.encode()), self._h)
+
+    # -- inspection
+    def population(self) -> int:
+        n = C.c_uint32(0)
+        check(lib().epi_engine_population(self._h, C.byref(n)), self._h)
+        return n.value
+
+    def snapshot(self) -> np.ndarray:
+        n = self.population()
+        out = np.zeros(n, dtype=AGENT_DTYPE)
+        check(lib().epi_engine_snapshot(self._h, out.ctypes.data, n), self._h)
+        return out
+
+    def geography(self) -> EpiGeography:
+        g = EpiGeography()
+        check(lib().epi_engine_geography(self._h, C.byref(g)), self._h)
+        return g
+
+    def check_invariants(self) -> None:
+        check(lib().epi_engine_check(self._h), self._h)
+
+    def set_stream(self, stream_ptr: int | None) -> None:
+        check(lib().epi_engine_set_stream(self._h, C.c_void_p(stream_ptr or 0)), self._h)
+
+    def set_profiling(self, on: bool) -> None:
+        check(lib().epi_engine_set_profiling(self._h, 1 if on else 0), self._h)
+
+    def kernel_stats(self) -> dict:
+        L = lib()
+        k = L.epi_engine_kernel_kinds()
+        launches = (C.c_uint32 * k)()
+        ms = (C.c_double * k)()
+        check(L.epi_engine_kernel_stats(self._h, launches, ms, k), self._h)
+        return {L.epi_engine_kernel_name(i).decode(): (launches[i], ms[i]) for i in range(k)}
+
+    def save_state(self) -> None:
+        check(lib().epi_engine_save_state(self._h), self._h)
+
+    def restore_state(self) -> None:
+        check(lib().epi_engine_restore_state(self._h), self._h)
+
+    def kernels_launched(self) -> int:
+        v = C.c_uint64(0)
+        check(lib().epi_engine_kernels_launched(self._h, C.byref(v)), self._h)
+        return v.value
+
+    def hour_bytes(self, hour: int) -> float:
+        b = C.c_double(0.0)
+        check(lib().epi_engine_hour_bytes(self._h, hour, C.byref(b)), self._h)
+        return b.value
