@@ -38,7 +38,7 @@ def _engine_rows(rows):
 TICK_CASES = {
     "small_pox": make_config(n=3000, grid=120, hours=24 * 30, seed=1, starting=(0, 0, 0, 20)),
     "covid_fast": make_config(n=3000, grid=120, hours=24 * 20, seed=2, disease=COVID_FAST, starting=(5, 5, 5, 20)),
-    "dense": make_config(n=9000, grid=120, hours=24 * 12, seed=3, disease=COVID_FAST, starting=(0, 0, 10, 30),
+    "dense": make_config(n=5500, grid=120, hours=24 * 12, seed=3, disease=COVID_FAST, starting=(0, 0, 10, 30),
                          pt=0.6, working=0.9),
 }
 
@@ -111,7 +111,7 @@ RUN_CASES = {
         n=5000, grid=120, hours=24 * 40, seed=6, disease=COVID_FAST, starting=(0, 0, 10, 30),
         interventions=[{"BuildNewHospital": {"spread_rate_threshold": 5}}]),
     "occupancy_hospital": make_config(
-        n=6000, grid=120, hours=24 * 40, seed=7, starting=(0, 0, 30, 30), occupancy=0.7,
+        n=5500, grid=120, hours=24 * 40, seed=7, starting=(0, 0, 30, 30), occupancy=0.7,
         interventions=[{"Lockdown": {"at_number_of_infections": 100, "essential_workers_population": 0.1}}]),
     "stop_early": make_config(n=800, grid=100, hours=24 * 60, seed=8, starting=(0, 0, 0, 1)),
 }
