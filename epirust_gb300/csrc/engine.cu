@@ -97,12 +97,15 @@ __global__ void __launch_bounds__(kThreads) k_decide(const DevParams* __restrict
                                                      const uint32_t* __restrict__ hour_base, uint32_t hour_offset,
                                                      int* err) {
     __shared__ uint32_t sh[8];
+    __shared__ DevParams sP;  // the parameter block, staged once per block
     if (threadIdx.x < 8) sh[threadIdx.x] = 0;
+    for (uint32_t k = threadIdx.x; k < sizeof(DevParams) / 4; k += blockDim.x)
+        reinterpret_cast<uint32_t*>(&sP)[k] = reinterpret_cast<const uint32_t*>(Pp)[k];
     __syncthreads();
-    const DevParams& P = *Pp;
+    const DevParams& P = sP;
     const uint32_t hour = *hour_base + hour_offset;
     const uint32_t hod = hour % 24u;
-    const PlaneView pl{plane, P.G, P.W, err};
+    const PlaneView pl{plane, P.G, P.WP, err};
     const uint32_t n = P.n;
     const uint32_t stride = gridDim.x * blockDim.x;
     uint32_t hosp_first = kNoAction;
@@ -163,20 +166,20 @@ __global__ void __launch_bounds__(kThreads) k_decide(const DevParams* __restrict
 __global__ void __launch_bounds__(kThreads) k_commit(const DevParams* __restrict__ Pp, uint32_t* __restrict__ pos,
                                                      const uint32_t* __restrict__ tgt, uint8_t* __restrict__ plane,
                                                      uint32_t* __restrict__ claim) {
-    const uint32_t n = Pp->n, W = (uint32_t)Pp->W;
+    const uint32_t n = Pp->n, W = (uint32_t)Pp->W, WP = (uint32_t)Pp->WP;
     const uint32_t stride = gridDim.x * blockDim.x;
     for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += stride) {
         const uint32_t t = tgt[i];
         if (t == kNoAction) continue;
         const uint32_t p = pos[i];
         const uint32_t xy = target_xy(t), cls = target_class(t);
-        const size_t old_cell = (size_t)unpack_y(p) * W + unpack_x(p);
+        const size_t old_cell = (size_t)(unpack_y(p) + 1) * WP + (unpack_x(p) + 1);
         if (xy != p) {
-            const size_t new_cell = (size_t)unpack_y(xy) * W + unpack_x(xy);
-            if (claim[new_cell] == i) {
-                claim[new_cell] = kNoClaim;
+            const size_t claim_cell = (size_t)unpack_y(xy) * W + unpack_x(xy);
+            if (claim[claim_cell] == i) {
+                claim[claim_cell] = kNoClaim;
                 plane[old_cell] = 0;
-                plane[new_cell] = (uint8_t)cls;
+                plane[(size_t)(unpack_y(xy) + 1) * WP + (unpack_x(xy) + 1)] = (uint8_t)cls;
                 pos[i] = xy;
                 continue;
             }
@@ -188,12 +191,12 @@ __global__ void __launch_bounds__(kThreads) k_commit(const DevParams* __restrict
 __global__ void k_build_plane(const DevParams* __restrict__ Pp, const uint32_t* __restrict__ pos,
                               const uint2* __restrict__ st, uint8_t* __restrict__ plane, int* err) {
     const uint32_t n = Pp->n;
-    const int32_t G = Pp->G, W = Pp->W;
+    const int32_t G = Pp->G, WP = Pp->WP;
     for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
         const uint32_t p = pos[i];
         const int32_t x = unpack_x(p), y = unpack_y(p);
         if (x > G || y > G) { atomicOr(err, 2); continue; }
-        plane[(size_t)y * W + x] = (uint8_t)cell_class(*Pp, st[i].x);
+        plane[(size_t)(y + 1) * WP + (x + 1)] = (uint8_t)cell_class(*Pp, st[i].x);
     }
 }
 
@@ -224,21 +227,21 @@ __global__ void k_check_agents(const DevParams* __restrict__ Pp, const uint32_t*
                                const uint2* __restrict__ st, const uint8_t* __restrict__ plane,
                                unsigned long long* bad) {
     const uint32_t n = Pp->n;
-    const int32_t G = Pp->G, W = Pp->W;
+    const int32_t G = Pp->G, WP = Pp->WP;
     for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
         const uint32_t p = pos[i];
         const int32_t x = unpack_x(p), y = unpack_y(p);
-        if (x > G || y > G || plane[(size_t)y * W + x] != cell_class(*Pp, st[i].x)) atomicAdd(bad, 1ull);
+        if (x > G || y > G || plane[(size_t)(y + 1) * WP + (x + 1)] != cell_class(*Pp, st[i].x)) atomicAdd(bad, 1ull);
     }
 }
 
-__global__ void k_check_plane(size_t cells, const uint8_t* __restrict__ plane, const uint32_t* __restrict__ claim,
-                              unsigned long long* occupied, unsigned long long* claimed) {
+__global__ void k_check_plane(size_t plane_bytes, const uint8_t* __restrict__ plane, size_t claim_cells,
+                              const uint32_t* __restrict__ claim, unsigned long long* occupied,
+                              unsigned long long* claimed) {
     unsigned long long o = 0, c = 0;
-    for (size_t k = blockIdx.x * (size_t)blockDim.x + threadIdx.x; k < cells; k += (size_t)gridDim.x * blockDim.x) {
-        o += plane[k] != 0;
-        c += claim[k] != kNoClaim;
-    }
+    const size_t stride = (size_t)gridDim.x * blockDim.x;
+    for (size_t k = blockIdx.x * (size_t)blockDim.x + threadIdx.x; k < plane_bytes; k += stride) o += plane[k] != 0;
+    for (size_t k = blockIdx.x * (size_t)blockDim.x + threadIdx.x; k < claim_cells; k += stride) c += claim[k] != kNoClaim;
     for (int off = 16; off; off >>= 1) {
         o += __shfl_down_sync(0xFFFFFFFFu, o, off);
         c += __shfl_down_sync(0xFFFFFFFFu, c, off);
@@ -260,8 +263,10 @@ struct epi_engine {
     epi_geography geo0{}, geo{};
     DevParams hp{};
     uint32_t n = 0;
-    size_t cells = 0;
-    int grid_blocks = 0;
+    size_t plane_bytes = 0;  // padded byte plane (G+3)^2 + slack
+    size_t claim_cells = 0;  // (G+1)^2
+    int grid_blocks = 0;    // resident grid of the counting kernels (grid-stride loops)
+    int commit_blocks = 0;  // one thread per agent
     // device
     DevParams* d_params = nullptr;
     uint32_t *d_pos = nullptr, *d_home = nullptr, *d_work = nullptr, *d_wsa = nullptr, *d_tgt = nullptr;
@@ -329,6 +334,7 @@ static void fill_dev_params(epi_engine* h) {
     d.n = h->n;
     d.G = (int32_t)p.grid_size;
     d.W = d.G + 1;
+    d.WP = d.G + 3;
     d.hosp_code = kHosp0;
     d.area[kTransport] = to_rect(h->geo0.transport);
     d.area[kHousing] = to_rect(h->geo0.housing);
@@ -427,7 +433,7 @@ static int enqueue_hours(epi_engine* h, uint32_t first_hour, uint32_t nh) {
             LAUNCH(kKDecide, (k_decide<<<blocks, kThreads, 0, h->stream>>>(
                                   h->d_params, h->d_pos, h->d_st, h->d_home, h->d_work, h->d_wsa, h->d_plane, h->d_claim,
                                   h->d_tgt, row, h->d_hour_base, k, h->d_err)));
-            LAUNCH(kKCommit, (k_commit<<<blocks, kThreads, 0, h->stream>>>(h->d_params, h->d_pos, h->d_tgt, h->d_plane,
+            LAUNCH(kKCommit, (k_commit<<<h->commit_blocks, kThreads, 0, h->stream>>>(h->d_params, h->d_pos, h->d_tgt, h->d_plane,
                                                                            h->d_claim)));
         }
     }
@@ -558,8 +564,8 @@ static int upload_world(epi_engine* h, const epi_agent_record* recs) {
     CK(cudaMemcpyAsync(h->d_work, work.data(), n * sizeof(uint32_t), cudaMemcpyHostToDevice, h->stream));
     CK(cudaMemcpyAsync(h->d_wsa, wsa.data(), n * sizeof(uint32_t), cudaMemcpyHostToDevice, h->stream));
     CK(cudaMemcpyAsync(h->d_st, st.data(), n * sizeof(uint2), cudaMemcpyHostToDevice, h->stream));
-    CK(cudaMemsetAsync(h->d_plane, 0, h->cells, h->stream));
-    CK(cudaMemsetAsync(h->d_claim, 0xFF, h->cells * sizeof(uint32_t), h->stream));
+    CK(cudaMemsetAsync(h->d_plane, 0, h->plane_bytes, h->stream));
+    CK(cudaMemsetAsync(h->d_claim, 0xFF, h->claim_cells * sizeof(uint32_t), h->stream));
     CK(cudaMemsetAsync(h->d_err, 0, sizeof(int), h->stream));
     LAUNCH(kKBuildPlane, (k_build_plane<<<h->grid_blocks, kThreads, 0, h->stream>>>(h->d_params, h->d_pos, h->d_st,
                                                                                       h->d_plane, h->d_err)));
@@ -580,7 +586,8 @@ static int engine_init(epi_engine* h, const epi_params& p, const epi_agent_recor
     h->geo = h->geo0;
     fill_dev_params(h);
     const size_t W = (size_t)p.grid_size + 1;
-    h->cells = W * W;
+    h->claim_cells = W * W;
+    h->plane_bytes = (W + 2) * (W + 2) + 16;  // border of one cell, 16 B slack for the row loads
     int dev = 0, sms = 0, per_sm = 0;
     CK(cudaGetDevice(&dev));
     CK(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev));
@@ -588,6 +595,7 @@ static int engine_init(epi_engine* h, const epi_params& p, const epi_agent_recor
     per_sm = std::max(per_sm, 1);
     const uint64_t need_blocks = ((uint64_t)n + kThreads - 1) / kThreads;
     h->grid_blocks = (int)std::min<uint64_t>(need_blocks, (uint64_t)sms * per_sm);
+    h->commit_blocks = (int)need_blocks;
     CK(cudaStreamCreateWithFlags(&h->stream, cudaStreamNonBlocking));
     h->own_stream = true;
     CK(cudaMalloc(&h->d_params, sizeof(DevParams)));
@@ -597,8 +605,8 @@ static int engine_init(epi_engine* h, const epi_params& p, const epi_agent_recor
     CK(cudaMalloc(&h->d_wsa, n * sizeof(uint32_t)));
     CK(cudaMalloc(&h->d_tgt, n * sizeof(uint32_t)));
     CK(cudaMalloc(&h->d_st, n * sizeof(uint2)));
-    CK(cudaMalloc(&h->d_plane, h->cells));
-    CK(cudaMalloc(&h->d_claim, h->cells * sizeof(uint32_t)));
+    CK(cudaMalloc(&h->d_plane, h->plane_bytes));
+    CK(cudaMalloc(&h->d_claim, h->claim_cells * sizeof(uint32_t)));
     CK(cudaMalloc(&h->d_hour_base, sizeof(uint32_t)));
     CK(cudaMalloc(&h->d_err, sizeof(int)));
     CK(cudaMalloc(&h->d_scratch, 4 * sizeof(unsigned long long)));
@@ -888,7 +896,7 @@ int epi_engine_check(epi_engine* h) {
     CK(cudaMemsetAsync(h->d_scratch, 0, 4 * sizeof(unsigned long long), h->stream));
     LAUNCH(kKCheck, (k_check_agents<<<h->grid_blocks, kThreads, 0, h->stream>>>(h->d_params, h->d_pos, h->d_st, h->d_plane,
                                                                                  h->d_scratch)));
-    LAUNCH(kKCheck, (k_check_plane<<<h->grid_blocks, kThreads, 0, h->stream>>>(h->cells, h->d_plane, h->d_claim,
+    LAUNCH(kKCheck, (k_check_plane<<<h->grid_blocks, kThreads, 0, h->stream>>>(h->plane_bytes, h->d_plane, h->claim_cells, h->d_claim,
                                                                                 h->d_scratch + 1, h->d_scratch + 2)));
     unsigned long long v[4] = {0, 0, 0, 0};
     CK(cudaMemcpyAsync(v, h->d_scratch, sizeof v, cudaMemcpyDeviceToHost, h->stream));
@@ -910,12 +918,12 @@ int epi_engine_save_state(epi_engine* h) {
         CK(cudaMalloc(&h->s_pos, n * sizeof(uint32_t)));
         CK(cudaMalloc(&h->s_wsa, n * sizeof(uint32_t)));
         CK(cudaMalloc(&h->s_st, n * sizeof(uint2)));
-        CK(cudaMalloc(&h->s_plane, h->cells));
+        CK(cudaMalloc(&h->s_plane, h->plane_bytes));
     }
     CK(cudaMemcpyAsync(h->s_pos, h->d_pos, n * sizeof(uint32_t), cudaMemcpyDeviceToDevice, h->stream));
     CK(cudaMemcpyAsync(h->s_wsa, h->d_wsa, n * sizeof(uint32_t), cudaMemcpyDeviceToDevice, h->stream));
     CK(cudaMemcpyAsync(h->s_st, h->d_st, n * sizeof(uint2), cudaMemcpyDeviceToDevice, h->stream));
-    CK(cudaMemcpyAsync(h->s_plane, h->d_plane, h->cells, cudaMemcpyDeviceToDevice, h->stream));
+    CK(cudaMemcpyAsync(h->s_plane, h->d_plane, h->plane_bytes, cudaMemcpyDeviceToDevice, h->stream));
     CK(cudaStreamSynchronize(h->stream));
     h->s_iv = h->iv;
     h->s_hosp_code = h->hp.hosp_code;
@@ -931,7 +939,7 @@ int epi_engine_restore_state(epi_engine* h) {
     CK(cudaMemcpyAsync(h->d_pos, h->s_pos, n * sizeof(uint32_t), cudaMemcpyDeviceToDevice, h->stream));
     CK(cudaMemcpyAsync(h->d_wsa, h->s_wsa, n * sizeof(uint32_t), cudaMemcpyDeviceToDevice, h->stream));
     CK(cudaMemcpyAsync(h->d_st, h->s_st, n * sizeof(uint2), cudaMemcpyDeviceToDevice, h->stream));
-    CK(cudaMemcpyAsync(h->d_plane, h->s_plane, h->cells, cudaMemcpyDeviceToDevice, h->stream));
+    CK(cudaMemcpyAsync(h->d_plane, h->s_plane, h->plane_bytes, cudaMemcpyDeviceToDevice, h->stream));
     h->iv = h->s_iv;
     h->geo = h->s_geo;
     if (h->hp.hosp_code != h->s_hosp_code) {
@@ -984,7 +992,7 @@ int epi_engine_hour_bytes(const epi_engine* h, uint32_t hour, double* bytes) {
     const uint32_t hod = hour % 24u;
     const double n = (double)h->n;
     if (hod >= 1u && hod <= 6u) *bytes = n * (hod == 1u ? 8.0 : 4.0);
-    else *bytes = n * 44.0 + (double)h->cells;
+    else *bytes = n * 44.0 + (double)h->claim_cells;
     return EPI_OK;
 }
 

@@ -8,10 +8,11 @@
 //   work[i]  start corner of the 10x10 office (packed like pos; the house for non-workers)
 //   wsa[i]   work_start_at of hospital staff (read only for staff)
 // The occupancy plane is one byte per cell of the (G+1) x (G+1) plane (the reference's
-// areas reach row and column G, engine/src/geography/mod.rs:42-48):
+// areas reach row and column G, engine/src/geography/mod.rs:42-48), stored with a one-cell
+// border of zeros (pitch and height G+3, cell (x, y) at (y+1) * (G+3) + x+1):
 //   0 = vacant, 1 = occupied and not infectious, 2 = infectious at the regular rate,
 //   3 = infectious at the high rate.
-// A u32 claim plane of the same extent resolves cell conflicts (lowest agent index wins).
+// A u32 claim plane of (G+1) x (G+1) resolves cell conflicts (lowest agent index wins).
 #pragma once
 
 #include <stdint.h>
@@ -73,7 +74,8 @@ EPI_HD bool rect_eq(const Rect& a, const Rect& b) { return a.x0 == b.x0 && a.y0 
 struct DevParams {
     uint32_t n;                 // agents
     int32_t G;                  // grid size
-    int32_t W;                  // plane width G + 1
+    int32_t W;                  // claim-plane width G + 1
+    int32_t WP;                 // byte-plane pitch G + 3 (one-cell border on each side)
     uint32_t hosp_code;         // kHosp0 or kHosp1: the current hospital_area
     Rect area[kNumAreas];       // global areas by code (HOME/WORK slots unused)
     uint32_t key0, key1;        // Philox key = seed

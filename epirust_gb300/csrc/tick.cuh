@@ -7,6 +7,13 @@
 // engine/src/state_machine/default_disease_handler.rs:31-103 and
 // engine/src/allocation_map.rs:136-163; random draws are fixed words of per-agent-hour
 // Philox blocks (counter = agent, hour, block, 0).
+//
+// Moore neighbourhoods are evaluated as bit masks: the byte plane carries a one-cell border,
+// so the 3x3 block around any cell of [0, G]^2 is in bounds; each of its three rows comes in
+// as two aligned 32-bit loads and a funnel shift, and SWAR tests turn the nine bytes into
+// 8-bit masks (bit k = k-th neighbour in NeighborIterator order) of occupied, infectious and
+// high-rate neighbours.  The area and grid filters of get_neighbors_of / is_point_in_grid
+// become a second mask built from six comparisons.
 #pragma once
 
 #include "epi_internal.h"
@@ -19,23 +26,66 @@ __device__ __forceinline__ int32_t nb_dx(int k) { return (int32_t)((0x9224u >> (
 __device__ __forceinline__ int32_t nb_dy(int k) { return (int32_t)((0xA940u >> (2 * k)) & 3u) - 1; }
 
 struct PlaneView {
-    const uint8_t* __restrict__ cells;
-    int32_t G, W;
+    const uint8_t* __restrict__ cells;  // padded plane: cell (x, y) at (y + 1) * WP + (x + 1)
+    int32_t G, WP;
     int* err;
-    // The only cells a rule can address lie in [0, G]^2 by construction; anything else is
+    // Cells outside [0, G]^2 are never addressed by construction; if one were, it is
     // reported through err and treated as occupied instead of being dereferenced.
+    __device__ __forceinline__ bool inside(int32_t x, int32_t y) const {
+        return (uint32_t)x <= (uint32_t)G && (uint32_t)y <= (uint32_t)G;
+    }
     __device__ __forceinline__ uint32_t at(int32_t x, int32_t y) const {
-        if ((uint32_t)x > (uint32_t)G || (uint32_t)y > (uint32_t)G) {
+        if (!inside(x, y)) {
             atomicOr(err, 1);
             return 1u;
         }
-        return __ldg(cells + (size_t)y * (size_t)W + (size_t)x);
+        return __ldg(cells + (size_t)(y + 1) * (size_t)WP + (size_t)(x + 1));
     }
     __device__ __forceinline__ bool vacant(int32_t x, int32_t y) const { return at(x, y) == 0u; }
-    __device__ __forceinline__ bool in_grid(int32_t x, int32_t y) const {
-        return x >= 0 && y >= 0 && x < G && y < G;  // is_point_in_grid, allocation_map.rs:156-159
+    // Bytes of (x-1, y), (x, y), (x+1, y) in bits 0-7, 8-15, 16-23.
+    __device__ __forceinline__ uint32_t row3(int32_t x, int32_t y) const {
+        const uintptr_t a = (uintptr_t)(cells + (size_t)(y + 1) * (size_t)WP + (size_t)x);
+        const uint32_t* w = (const uint32_t*)(a & ~(uintptr_t)3);
+        const uint32_t lo = __ldg(w), hi = __ldg(w + 1);
+        return __funnelshift_r(lo, hi, (uint32_t)(a & 3u) * 8u) & 0xFFFFFFu;
     }
 };
+
+// 8-bit masks of the Moore neighbourhood of one cell.
+struct Nbhd {
+    uint32_t occupied, infectious, high;
+};
+
+// Gather the per-byte flag bits (bits 0, 8, 16 of each row) into NeighborIterator order.
+__device__ __forceinline__ uint32_t gather8(uint32_t f0, uint32_t f1, uint32_t f2) {
+    return (f0 & 1u) | ((f0 >> 7) & 2u) | ((f0 >> 14) & 4u) | ((f1 & 1u) << 3) | ((f1 >> 12) & 16u) |
+           ((f2 & 1u) << 5) | ((f2 >> 2) & 64u) | ((f2 >> 9) & 128u);
+}
+
+// Plane bytes are 0..3: occupied <=> bit0|bit1, infectious <=> bit1, high rate <=> bit0&bit1.
+__device__ __forceinline__ Nbhd neighbourhood(const PlaneView& pl, int32_t x, int32_t y) {
+    if (!pl.inside(x, y)) {
+        atomicOr(pl.err, 1);
+        return Nbhd{0xFFu, 0u, 0u};
+    }
+    const uint32_t r0 = pl.row3(x, y - 1), r1 = pl.row3(x, y), r2 = pl.row3(x, y + 1);
+    const uint32_t m = 0x010101u;
+    Nbhd n;
+    n.occupied = gather8((r0 | (r0 >> 1)) & m, (r1 | (r1 >> 1)) & m, (r2 | (r2 >> 1)) & m);
+    n.infectious = gather8((r0 >> 1) & m, (r1 >> 1) & m, (r2 >> 1) & m);
+    n.high = gather8(r0 & (r0 >> 1) & m, r1 & (r1 >> 1) & m, r2 & (r2 >> 1) & m);
+    return n;
+}
+
+// Neighbours of (x, y) inside area a and the grid (Area::get_neighbors_of filtered by
+// is_point_in_grid), as a mask in NeighborIterator order.
+__device__ __forceinline__ uint32_t valid_neighbours(const Rect& a, int32_t G, int32_t x, int32_t y) {
+    const int32_t lx = max(a.x0, 0), hx = min(a.x1, G - 1), ly = max(a.y0, 0), hy = min(a.y1, G - 1);
+    const uint32_t cl = (x - 1 >= lx) & (x - 1 <= hx), cc = (x >= lx) & (x <= hx), cr = (x + 1 >= lx) & (x + 1 <= hx);
+    const uint32_t rt = (y - 1 >= ly) & (y - 1 <= hy), rm = (y >= ly) & (y <= hy), rb = (y + 1 >= ly) & (y + 1 <= hy);
+    return (cl & rt) | ((cc & rt) << 1) | ((cr & rt) << 2) | ((cl & rm) << 3) | ((cr & rm) << 4) | ((cl & rb) << 5) |
+           ((cc & rb) << 6) | ((cr & rb) << 7);
+}
 
 // Lazily materialised Philox blocks of one agent-hour.
 struct Draws {
@@ -92,26 +142,17 @@ __device__ __forceinline__ uint32_t cell_class(const DevParams& P, uint32_t s) {
     return 1u + rate_class(P.reg_start, P.high_start, P.last_day, d);
 }
 
-// Citizen::move_agent_from, citizen/mod.rs:415-432
+// Citizen::move_agent_from, citizen/mod.rs:415-432: uniform choice among the vacant
+// neighbours (of the cell, or of a random point of the area when outside it).
 __device__ __forceinline__ Cell move_agent_from(const PlaneView& pl, uint32_t s, const Rect& cur, Cell cell, Draws& dr) {
     if (!can_move(s)) return cell;
     Cell c = cell;
     if (!rect_has(cur, cell.x, cell.y)) c = random_point(cur, dr.m(0), dr.m(1));
-    uint32_t mask = 0;
-#pragma unroll
-    for (int k = 0; k < 8; ++k) {
-        int32_t qx = c.x + nb_dx(k), qy = c.y + nb_dy(k);
-        if (rect_has(cur, qx, qy) && pl.in_grid(qx, qy) && pl.vacant(qx, qy)) mask |= 1u << k;
-    }
-    if (!mask) return cell;
-    uint32_t j = uniform_index(dr.m(2), (uint32_t)__popc(mask));
-    // position of the j-th set bit
-    uint32_t m = mask;
-#pragma unroll
-    for (int t = 0; t < 7; ++t)
-        if (t < (int)j) m &= m - 1u;
-    int k = __ffs(m) - 1;
-    return Cell{c.x + nb_dx(k), c.y + nb_dy(k)};  // vacant by construction: move_agent keeps it
+    const uint32_t cand = valid_neighbours(cur, pl.G, c.x, c.y) & ~neighbourhood(pl, c.x, c.y).occupied;
+    if (!cand) return cell;
+    const uint32_t j = uniform_index(dr.m(2), (uint32_t)__popc(cand));
+    const int k = (int)__fns(cand, 0u, (int)j + 1);  // position of the j-th set bit
+    return Cell{c.x + nb_dx(k), c.y + nb_dy(k)};     // vacant by construction: move_agent keeps it
 }
 
 // Citizen::goto_area, citizen/mod.rs:367-395
@@ -139,14 +180,16 @@ __device__ __forceinline__ void infection_dynamics(const DevParams& P, const Pla
     const uint32_t v = s & kStateMask;
     if (v == EPI_S) {
         if (s & (kWq | kVacc)) return;
+        const Nbhd nb = neighbourhood(pl, cell.x, cell.y);
+        uint32_t cand = valid_neighbours(cur, pl.G, cell.x, cell.y) & nb.infectious;
+        if (!cand) return;  // no infectious occupant among the neighbours: no draw can succeed
+        const uint64_t thr_reg = P.thr_rate[1], thr_high = P.thr_rate[2];
+        // neighbours in NeighborIterator order; the first successful Bernoulli exposes
 #pragma unroll
         for (int k = 0; k < 8; ++k) {
-            int32_t qx = cell.x + nb_dx(k), qy = cell.y + nb_dy(k);
-            if (!rect_has(cur, qx, qy) || !pl.in_grid(qx, qy)) continue;
-            uint32_t b = pl.at(qx, qy);
-            if (b < 2u) continue;
-            uint32_t u = k < 4 ? dr.d(k) : dr.d2(k - 4);
-            if ((uint64_t)u < P.thr_rate[b - 1u]) {
+            if (!((cand >> k) & 1u)) continue;
+            const uint32_t u = k < 4 ? dr.d(k) : dr.d2(k - 4);
+            if ((uint64_t)u < (((nb.high >> k) & 1u) ? thr_high : thr_reg)) {
                 s = with_state(s, EPI_E);
                 at = hour;
                 return;
