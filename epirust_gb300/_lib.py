@@ -100,7 +100,7 @@ EXPORTS = [
     "epi_engine_write_outputs", "epi_engine_population", "epi_engine_snapshot", "epi_engine_geography",
     "epi_engine_check", "epi_engine_set_profiling", "epi_engine_kernel_stats", "epi_engine_kernel_name",
     "epi_engine_kernel_kinds", "epi_abi_struct_size", "epi_engine_hour_bytes", "epi_engine_save_state",
-    "epi_engine_restore_state", "epi_engine_kernels_launched",
+    "epi_engine_restore_state", "epi_engine_kernels_launched", "epi_tick_hour_noalloc",
 ]
 
 _lib = None
@@ -162,6 +162,7 @@ def lib():
     _sig(L, "epi_engine_save_state", C.c_int, [V])
     _sig(L, "epi_engine_restore_state", C.c_int, [V])
     _sig(L, "epi_engine_kernels_launched", C.c_int, [V, P(C.c_uint64)])
+    _sig(L, "epi_tick_hour_noalloc", C.c_int, [P(EpiParams), C.c_uint32, C.c_uint32, V, V, V, V, V, V, V, V])
     _lib = L
     return L
 

@@ -14,6 +14,7 @@
 #include <cstring>
 #include <map>
 #include <memory>
+#include <mutex>
 #include <string>
 #include <utility>
 #include <vector>
@@ -997,3 +998,149 @@ int epi_engine_hour_bytes(const epi_engine* h, uint32_t hour, double* bytes) {
 }
 
 }  // extern "C"
+
+// ------------------------------------------------------------------ no-allocation hour
+// epi_tick_hour_noalloc: one simulated hour on device arrays the caller owns, for callers
+// that cannot allocate device memory (see include/epi_engine.h).  Its scratch -- the
+// parameter block, the hour word, the error word, the per-agent proposal buffer and the
+// (G+1)^2 claim plane -- lives in the file-scope array below, which every GPU that loads
+// this library holds until the process exits.  All calls share it: calls whose work overlaps
+// on the GPU (two streams, two host threads) race on it and must be serialised by the caller.
+namespace {
+
+constexpr size_t kNoAllocScratchBytes = size_t(48) << 20;  // 48 MiB
+constexpr size_t kNoAllocParamsOff = 0;                     // DevParams
+constexpr size_t kNoAllocHourOff = 256;                     // u32 hour
+constexpr size_t kNoAllocErrOff = 260;                      // int error flags
+constexpr size_t kNoAllocTgtOff = 512;                      // u32 per agent
+static_assert(sizeof(DevParams) <= kNoAllocHourOff, "parameter block must fit its slot");
+
+__device__ __align__(256) unsigned char g_noalloc_scratch[kNoAllocScratchBytes];
+
+struct NoAllocDevice {
+    unsigned char* base = nullptr;  // device address of g_noalloc_scratch on this device
+    int grid_blocks = 0;            // resident grid of k_decide / k_sleep
+};
+constexpr int kNoAllocMaxDevices = 64;
+NoAllocDevice g_noalloc_devices[kNoAllocMaxDevices];
+std::mutex g_noalloc_mutex;
+
+size_t align256(size_t v) { return (v + 255) & ~size_t(255); }
+
+DevParams noalloc_params(const epi_params& p, uint32_t hospital_grown) {
+    epi_geography g = define_geography(p.grid_size);
+    resize_hospital(g, (int32_t)p.number_of_agents, 0.002, p.hospital_beds_percentage);
+    DevParams d;
+    std::memset(&d, 0, sizeof d);
+    d.n = p.number_of_agents;
+    d.G = (int32_t)p.grid_size;
+    d.W = d.G + 1;
+    d.WP = d.G + 3;
+    d.area[kTransport] = to_rect(g.transport);
+    d.area[kHousing] = to_rect(g.housing);
+    d.area[kHosp0] = to_rect(g.hospital);
+    d.area[kHosp1] = to_rect(grown_hospital(g));
+    d.hosp_code = (hospital_grown && !rect_eq(d.area[kHosp1], d.area[kHosp0])) ? kHosp1 : kHosp0;
+    d.key0 = (uint32_t)p.seed;
+    d.key1 = (uint32_t)(p.seed >> 32);
+    d.reg_start = p.regular_transmission_start_day;
+    d.high_start = p.high_transmission_start_day;
+    d.last_day = p.last_day;
+    d.exposed_duration = p.exposed_duration;
+    d.pre_duration = p.pre_symptomatic_duration;
+    const double rates[3] = {0.0, p.regular_transmission_rate, p.high_transmission_rate};
+    for (int c = 0; c < 3; ++c) {
+        d.thr_rate[c] = bernoulli_threshold(rates[c]);
+        if (rates[c] >= p.high_transmission_rate) d.hosp_if_class |= 1u << c;
+    }
+    d.thr_death = bernoulli_threshold(p.death_rate);
+    d.thr_symptoms = bernoulli_threshold(1.0 - p.percentage_asymptomatic_population);
+    d.thr_severe = bernoulli_threshold(p.percentage_severe_infected_population);
+    return d;
+}
+
+int noalloc_fail(int rc, const std::string& msg) {
+    g_create_error = msg;
+    return rc;
+}
+
+#define NOALLOC_CK(call)                                                                     \
+    do {                                                                                     \
+        cudaError_t e_ = (call);                                                             \
+        if (e_ != cudaSuccess) return noalloc_fail(EPI_ERR_CUDA, std::string(#call) + ": " + cudaGetErrorString(e_)); \
+    } while (0)
+
+// Once per device, with that device current: the device address of the scratch array (the
+// host-side symbol is only a stand-in) and the launch shape.
+int noalloc_setup(int dev, NoAllocDevice** out) {
+    std::lock_guard<std::mutex> lock(g_noalloc_mutex);
+    NoAllocDevice& d = g_noalloc_devices[dev];
+    if (!d.base) {
+        void* ptr = nullptr;
+        NOALLOC_CK(cudaGetSymbolAddress(&ptr, g_noalloc_scratch));
+        int sms = 0, per_sm = 0;
+        NOALLOC_CK(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev));
+        NOALLOC_CK(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_decide, kThreads, 0));
+        d.grid_blocks = sms * std::max(per_sm, 1);
+        d.base = static_cast<unsigned char*>(ptr);
+    }
+    *out = &d;
+    return EPI_OK;
+}
+
+}  // namespace
+
+extern "C" int epi_tick_hour_noalloc(const epi_params* params, uint32_t hour, uint32_t hospital_grown, uint32_t* pos,
+                                     uint32_t* state, const uint32_t* home, const uint32_t* work, uint32_t* work_start_at,
+                                     uint8_t* plane, uint32_t* counts, void* cuda_stream) {
+    if (!params || !pos || !state || !home || !work || !work_start_at || !plane || !counts)
+        return noalloc_fail(EPI_ERR_ARG, "epi_tick_hour_noalloc: null pointer argument");
+    if (reinterpret_cast<uintptr_t>(state) % 8 != 0)
+        return noalloc_fail(EPI_ERR_ARG, "epi_tick_hour_noalloc: state must be 8-byte aligned (two words per agent)");
+    const std::string bad = validate_params(*params);
+    if (!bad.empty()) return noalloc_fail(EPI_ERR_CONFIG, bad);
+    const uint32_t n = params->number_of_agents;
+    const size_t side = (size_t)params->grid_size + 1;
+    const size_t claim_off = align256(kNoAllocTgtOff + (size_t)n * sizeof(uint32_t));
+    const size_t claim_bytes = side * side * sizeof(uint32_t);
+    if (claim_off + claim_bytes > kNoAllocScratchBytes)
+        return noalloc_fail(EPI_ERR_CAPACITY,
+                            "epi_tick_hour_noalloc: " + std::to_string(n) + " agents on a grid of " +
+                                std::to_string(params->grid_size) + " need " + std::to_string(claim_off + claim_bytes) +
+                                " bytes of scratch; the fixed maximum is " + std::to_string(kNoAllocScratchBytes));
+    int dev = 0;
+    NOALLOC_CK(cudaGetDevice(&dev));
+    if (dev < 0 || dev >= kNoAllocMaxDevices) return noalloc_fail(EPI_ERR_ARG, "epi_tick_hour_noalloc: device index too large");
+    NoAllocDevice* d = nullptr;
+    int rc = noalloc_setup(dev, &d);
+    if (rc) return rc;
+    cudaStream_t s = static_cast<cudaStream_t>(cuda_stream);
+    const DevParams hp = noalloc_params(*params, hospital_grown);
+    DevParams* d_params = reinterpret_cast<DevParams*>(d->base + kNoAllocParamsOff);
+    uint32_t* d_hour = reinterpret_cast<uint32_t*>(d->base + kNoAllocHourOff);
+    int* d_err = reinterpret_cast<int*>(d->base + kNoAllocErrOff);
+    uint32_t* d_tgt = reinterpret_cast<uint32_t*>(d->base + kNoAllocTgtOff);
+    uint32_t* d_claim = reinterpret_cast<uint32_t*>(d->base + claim_off);
+    // every call starts from clean scratch: the claim plane free, the error word zero
+    NOALLOC_CK(cudaMemcpyAsync(d_params, &hp, sizeof hp, cudaMemcpyHostToDevice, s));
+    NOALLOC_CK(cudaMemcpyAsync(d_hour, &hour, sizeof hour, cudaMemcpyHostToDevice, s));
+    NOALLOC_CK(cudaMemsetAsync(d_err, 0, sizeof(int), s));
+    NOALLOC_CK(cudaMemsetAsync(counts, 0, 8 * sizeof(uint32_t), s));
+    uint2* st = reinterpret_cast<uint2*>(state);
+    const int blocks = (int)std::min<uint64_t>(((uint64_t)n + kThreads - 1) / kThreads, (uint64_t)d->grid_blocks);
+    const uint32_t hod = hour % 24u;
+    if (hod >= 1u && hod <= 6u) {
+        k_sleep<<<blocks, kThreads, 0, s>>>(d_params, st, counts);
+    } else {
+        NOALLOC_CK(cudaMemsetAsync(d_claim, 0xFF, claim_bytes, s));
+        k_decide<<<blocks, kThreads, 0, s>>>(d_params, pos, st, home, work, work_start_at, plane, d_claim, d_tgt, counts,
+                                             d_hour, 0u, d_err);
+        k_commit<<<(int)(((uint64_t)n + kThreads - 1) / kThreads), kThreads, 0, s>>>(d_params, pos, d_tgt, plane, d_claim);
+    }
+    NOALLOC_CK(cudaGetLastError());
+    int err = 0;
+    NOALLOC_CK(cudaMemcpyAsync(&err, d_err, sizeof err, cudaMemcpyDeviceToHost, s));
+    NOALLOC_CK(cudaStreamSynchronize(s));
+    if (err) return noalloc_fail(EPI_ERR_INVARIANT, "epi_tick_hour_noalloc: a rule addressed a cell outside the plane");
+    return EPI_OK;
+}

@@ -265,6 +265,44 @@ size_t epi_abi_struct_size(const char* name);
 /* Algorithmic bytes of one hour at the current state (the roofline numerator). */
 int epi_engine_hour_bytes(const epi_engine* h, uint32_t hour, double* bytes);
 
+/* ---------------------------------------------------------------- no-allocation hour */
+/* No counterpart in the reference.  One simulated hour (the work of epi_engine_simulate) on
+ * device arrays that the caller owns, for callers that cannot allocate device memory: a host
+ * runtime whose device memory comes from its own fixed pool or arena and may not grow behind
+ * its back, code recording a CUDA graph (cudaMalloc may not be called while a stream is being
+ * captured), or a real-time loop that must not enter the driver's allocator.  This entry
+ * point calls no cudaMalloc, cudaFree or allocating library routine; its scratch (parameter
+ * block, per-agent proposal buffer, (G+1)^2 claim plane) is one fixed 48 MiB device array
+ * inside the library, which every GPU that loads the library holds until the process exits.
+ * A world needs 512 + 4 N bytes of it, rounded up to a multiple of 256, plus 4 (G+1)^2 bytes;
+ * a larger one is rejected with EPI_ERR_CAPACITY and a message from
+ * epi_engine_last_error(NULL) -- e.g. 1,000,000 agents on a 2,500 grid fit (29 MB),
+ * 1,000,000 agents on a 3,500 grid (53 MB) do not.
+ *
+ * Arrays (device pointers, n = params->number_of_agents, G = params->grid_size), in the
+ * engine's packed layout, updated in place:
+ *   pos[n]            x | y << 16
+ *   state[2n]         per agent: word 0 = disease state (bits 0-2), hospitalized (3),
+ *                     isolated (4), vaccinated (5), work-quarantined (6), public transport (7),
+ *                     current-area code (8-10: 0 home, 1 office, 2 transport strip, 3 housing
+ *                     strip, 4 hospital, 5 grown hospital), work status (11-12), immunity + 2
+ *                     (13-15), infection day (16-31); word 1 = at_hour.  8-byte aligned.
+ *   home[n], work[n]  start corners of the 2x2 house / 10x10 office, packed like pos (read only)
+ *   work_start_at[n]  hospital staff schedule
+ *   plane[(G+3)^2+16] one byte per cell with a one-cell border: cell (x, y) at
+ *                     (y+1)*(G+3) + x+1; 0 vacant, 1 occupied, 2/3 infectious at the regular /
+ *                     high rate; border and slack bytes zero
+ *   counts[8]         out: S, E, I, H, R, D of this hour in counts[0..5]
+ * hospital_grown = 1 once BuildNewHospital has fired.  The call is issued on cuda_stream
+ * (NULL = the legacy default stream) and returns after the hour has finished.  The first call
+ * on a device looks up the scratch array's device address and the launch shape while that
+ * device is current; make it before any stream capture.  Every call shares the scratch array
+ * and starts by clearing the parts that must start clean, so calls in a row are independent;
+ * calls whose work overlaps on the GPU (other streams, other host threads) race on it. */
+int epi_tick_hour_noalloc(const epi_params* params, uint32_t hour, uint32_t hospital_grown, uint32_t* pos,
+                          uint32_t* state, const uint32_t* home, const uint32_t* work, uint32_t* work_start_at,
+                          uint8_t* plane, uint32_t* counts, void* cuda_stream);
+
 #ifdef __cplusplus
 }
 #endif
