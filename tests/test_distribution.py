@@ -1,0 +1,105 @@
+"""Distributional agreement with the reference's order semantics.
+
+The reference resolves cell conflicts in hash-map iteration order with an unseeded RNG, so
+its trajectories can only be matched in distribution.  O2 (oracle/o2.c) runs the reference's
+data flow -- FNV hash map keyed by cell, threaded map phase over the map, serial first-come
+resolve in that order -- with its own random stream.  Over many seeds, the epidemic curves
+of the engine semantics (lowest index wins; O1 on the CPU, the CUDA engine on the GPU) must
+match O2's: peak height, peak day and final attack rate agree within a 4-sigma band of the
+difference of means, and a two-sample Kolmogorov-Smirnov test does not reject (p > 1e-3).
+"""
+import json
+import multiprocessing as mp
+
+import numpy as np
+import pytest
+
+from helpers import make_config
+
+SMALL_POX_FAST = {
+    "regular_transmission_start_day": 2, "high_transmission_start_day": 5, "last_day": 9,
+    "asymptomatic_last_day": 22, "mild_infected_last_day": 22,
+    "regular_transmission_rate": 0.06, "high_transmission_rate": 0.2, "death_rate": 0.2,
+    "percentage_asymptomatic_population": 0.2, "percentage_severe_infected_population": 0.5,
+    "exposed_duration": 12, "pre_symptomatic_duration": 12,
+}
+
+
+def _config(n, grid, seed, hours):
+    return make_config(n=n, grid=grid, hours=hours, seed=seed, disease=SMALL_POX_FAST, starting=(0, 0, 0, 10),
+                       interventions=[{"Lockdown": {"at_number_of_infections": n // 20,
+                                                    "essential_workers_population": 0.2}}])
+
+
+def _summary(rows, n):
+    """(peak active cases, hour of the peak, final attack rate)."""
+    active = rows["exposed"].astype(np.int64) + rows["infected"] + rows["hospitalized"]
+    k = int(np.argmax(active))
+    last = rows[-1]
+    attack = (int(last["recovered"]) + int(last["deceased"]) + int(active[-1])) / n
+    return float(active[k]), float(rows["hour"][k]), attack
+
+
+def _o2_run(args):
+    n, grid, seed, hours = args
+    from oracle import oracle
+    from epirust_gb300 import Config
+    from epirust_gb300.engine import world_build
+
+    cfg = _config(n, grid, seed, hours)
+    recs, _ = world_build(Config(json.dumps(cfg)).params)
+    sim = oracle.O2(oracle.params_from_config(cfg), recs, threads=1)
+    return _summary(sim.run(1, hours, interventions=True, stop=True), n)
+
+
+def _o1_run(args):
+    n, grid, seed, hours = args
+    from oracle import oracle
+
+    cfg = _config(n, grid, seed, hours)
+    sim = oracle.O1(oracle.params_from_config(cfg))
+    return _summary(sim.run(1, hours, interventions=True, stop=True), n)
+
+
+def _pool_map(fn, jobs):
+    ctx = mp.get_context("spawn")
+    with ctx.Pool(processes=min(8, mp.cpu_count() or 1)) as pool:
+        return np.array(pool.map(fn, jobs))
+
+
+def _compare(a, b):
+    from scipy import stats
+
+    for j, name in enumerate(("peak", "peak_hour", "attack")):
+        x, y = a[:, j], b[:, j]
+        se = np.sqrt(x.var(ddof=1) / len(x) + y.var(ddof=1) / len(y)) + 1e-9
+        assert abs(x.mean() - y.mean()) < 4 * se, (name, x.mean(), y.mean(), se)
+        assert stats.ks_2samp(x, y).pvalue > 1e-3, (name, stats.ks_2samp(x, y))
+
+
+def test_o1_matches_reference_order_semantics_in_distribution(engine_built, oracle_mod):
+    """CPU: O1 (lowest index wins) vs O2 (hash order), 48 seeds each, independent streams."""
+    pytest.importorskip("scipy")
+    n, grid, hours = 1200, 60, 24 * 40
+    a = _pool_map(_o1_run, [(n, grid, 1000 + s, hours) for s in range(48)])
+    b = _pool_map(_o2_run, [(n, grid, 5000 + s, hours) for s in range(48)])
+    assert a[:, 2].mean() > 0.2  # epidemics take off
+    _compare(a, b)
+
+
+@pytest.mark.gpu
+def test_engine_matches_reference_order_semantics_in_distribution(gpu, oracle_mod):
+    """GPU engine vs O2 over 200 seeds each (peak, peak hour, attack rate)."""
+    pytest.importorskip("scipy")
+    from epirust_gb300 import Config, Epidemiology
+
+    n, grid, hours = 2000, 80, 24 * 40
+    b = _pool_map(_o2_run, [(n, grid, 9000 + s, hours) for s in range(200)])
+    a = []
+    for s in range(200):
+        eng = Epidemiology(Config(json.dumps(_config(n, grid, 100 + s, hours))))
+        a.append(_summary(eng.run(), n))
+        eng.close()
+    a = np.array(a)
+    assert a[:, 2].mean() > 0.2
+    _compare(a, b)
