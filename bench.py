@@ -174,6 +174,43 @@ def run_reference(args, cfg):
     print(json.dumps(line), flush=True)
 
 
+def run_batched(args, stream, flush) -> dict:
+    """Config 3: 256 replicates (10k-500k agents, sqrt grids, 2,400 h) in one launch per hour."""
+    import torch
+
+    from epirust_gb300 import Ensemble
+    from epirust_gb300.workloads import ensemble_params
+
+    params = ensemble_params(replicates=args.replicates)
+    agents = sum(p.number_of_agents for p in params)
+    t0 = time.perf_counter()
+    ens = Ensemble(params)
+    build_s = time.perf_counter() - t0
+    ens.set_stream(stream.cuda_stream)
+    ens.save_state()
+    for _ in range(1):
+        ens.restore_state()
+        ens.run()
+    steps = max(1, min(args.steps, 3))
+    ms_total, agent_hours = 0.0, 0.0
+    for k in range(steps):
+        with torch.cuda.stream(stream):
+            flush.fill_(k & 0xFF)
+        ev0, ev1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        ev0.record(stream)
+        ens.restore_state()
+        rows = ens.run()
+        ev1.record(stream)
+        ev1.synchronize()
+        ms_total += ev0.elapsed_time(ev1)
+        agent_hours += sum(float(p.number_of_agents) * len(r) for p, r in zip(params, rows))
+    ens.close()
+    return {"value": agent_hours / (ms_total / 1000.0), "unit": METRIC, "replicates": len(params), "agents": agents,
+            "ms_per_step": ms_total / steps, "steps": steps, "world_build_and_upload_s": build_s,
+            "workload": "256 replicates, populations log-uniform in [10k, 500k], grid ceil(sqrt(N/0.16)), regular "
+                        "rate U[0.02, 0.10], 0.05% exposed, 2400 h, no interventions, seeds from 11"}
+
+
 def run_gpu(args, cfg):
     import numpy as np
     import torch
@@ -290,6 +327,8 @@ def run_gpu(args, cfg):
         with open(tpath) as f:
             traffic = json.load(f).get("bytes_per_launch")
 
+    batched = run_batched(args, stream, flush) if not args.no_batched else None
+
     cpu = cpu_baseline(cfg, records, seconds=args.cpu_seconds) if rank == 0 and not args.no_cpu else None
 
     if rank == 0:
@@ -312,7 +351,10 @@ def run_gpu(args, cfg):
                     "d2h_bytes_per_step": int(hours_per_step * 32), "steps": e2e_steps},
             "gpu_launches": int(launches),
             "clocks": clocks,
+            "batched": batched,
         }
+        if batched:
+            batched["speedup_vs_plain"] = batched["value"] / value
         print(json.dumps(line), flush=True)
     if world > 1:
         import torch.distributed as dist
@@ -330,6 +372,8 @@ def main():
     ap.add_argument("--cpu-seconds", type=float, default=12.0)
     ap.add_argument("--ref-hours", type=int, default=24)
     ap.add_argument("--no-cpu", action="store_true")
+    ap.add_argument("--no-batched", action="store_true")
+    ap.add_argument("--replicates", type=int, default=256)
     args = ap.parse_args()
     with open(args.config) as f:
         cfg = json.load(f)

@@ -6,4 +6,4 @@ CUDA kernels behind the C ABI of include/epi_engine.h; this package is the Pytho
 that ABI.
 """
 from ._lib import AGENT_DTYPE, COUNTS_DTYPE, EpiError, EpiParams, lib  # noqa: F401
-from .engine import Config, Counts, Epidemiology, define_geography, world_build  # noqa: F401
+from .engine import Config, Counts, Ensemble, Epidemiology, define_geography, world_build  # noqa: F401

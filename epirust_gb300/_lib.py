@@ -101,6 +101,10 @@ EXPORTS = [
     "epi_engine_check", "epi_engine_set_profiling", "epi_engine_kernel_stats", "epi_engine_kernel_name",
     "epi_engine_kernel_kinds", "epi_abi_struct_size", "epi_engine_hour_bytes", "epi_engine_save_state",
     "epi_engine_restore_state", "epi_engine_kernels_launched", "epi_tick_hour_noalloc",
+    "epi_ensemble_create", "epi_ensemble_destroy", "epi_ensemble_last_error", "epi_ensemble_set_stream",
+    "epi_ensemble_replicates", "epi_ensemble_run", "epi_ensemble_snapshot", "epi_ensemble_check",
+    "epi_ensemble_save_state", "epi_ensemble_restore_state", "epi_ensemble_set_profiling", "epi_ensemble_kernel_stats",
+    "epi_ensemble_kernels_launched", "epi_ensemble_hour_bytes",
 ]
 
 _lib = None
@@ -162,6 +166,20 @@ def lib():
     _sig(L, "epi_engine_save_state", C.c_int, [V])
     _sig(L, "epi_engine_restore_state", C.c_int, [V])
     _sig(L, "epi_engine_kernels_launched", C.c_int, [V, P(C.c_uint64)])
+    _sig(L, "epi_ensemble_create", C.c_int, [V, C.c_uint32, P(V)])
+    _sig(L, "epi_ensemble_destroy", None, [V])
+    _sig(L, "epi_ensemble_last_error", C.c_char_p, [V])
+    _sig(L, "epi_ensemble_set_stream", C.c_int, [V, V])
+    _sig(L, "epi_ensemble_replicates", C.c_int, [V, P(C.c_uint32)])
+    _sig(L, "epi_ensemble_run", C.c_int, [V, V, C.c_uint32, V])
+    _sig(L, "epi_ensemble_snapshot", C.c_int, [V, C.c_uint32, V, C.c_size_t])
+    _sig(L, "epi_ensemble_check", C.c_int, [V])
+    _sig(L, "epi_ensemble_save_state", C.c_int, [V])
+    _sig(L, "epi_ensemble_restore_state", C.c_int, [V])
+    _sig(L, "epi_ensemble_set_profiling", C.c_int, [V, C.c_int])
+    _sig(L, "epi_ensemble_kernel_stats", C.c_int, [V, P(C.c_uint32), P(C.c_double), C.c_int])
+    _sig(L, "epi_ensemble_kernels_launched", C.c_int, [V, P(C.c_uint64)])
+    _sig(L, "epi_ensemble_hour_bytes", C.c_int, [V, C.c_uint32, P(C.c_double)])
     _sig(L, "epi_tick_hour_noalloc", C.c_int, [P(EpiParams), C.c_uint32, C.c_uint32, V, V, V, V, V, V, V, V])
     _lib = L
     return L

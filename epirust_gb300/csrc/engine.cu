@@ -1,12 +1,11 @@
-// engine.cu -- the GB300 engine tick: kernels, the engine handle and the C ABI.
+// engine.cu -- the engine handle and the C ABI of the GB300 tick.
 //
-// Per simulated hour (CitizenLocationMap::simulate, engine/src/allocation_map.rs:67-129):
-//   hours 1..6 of a day   k_sleep   current_area = home (non-staff), counts
-//   other hours           k_decide  per-agent rules on the previous-hour plane, proposals,
-//                                   atomicMin claims on the target cells, counts
-//                         k_commit  lowest claimant moves, losers stay, plane bytes updated,
-//                                   claims released
-// Hour segments between intervention points run as one captured CUDA graph.
+// An engine holds R worlds ("replicates") on one device: their agents are concatenated in
+// 256-slot chunks, their bordered byte planes and claim planes laid end to end, and every
+// kernel of kernels.cuh serves all of them in one launch per hour.  The single-engine API
+// (epi_engine_*) is the R = 1 case; the ensemble API (epi_ensemble_*) runs many replicates
+// of uneven population and grid size in lockstep.  Hour segments between intervention
+// points run as one captured CUDA graph, replayed with the first hour read on the device.
 #include <cuda_runtime.h>
 
 #include <algorithm>
@@ -16,277 +15,60 @@
 #include <memory>
 #include <mutex>
 #include <string>
+#include <thread>
 #include <utility>
 #include <vector>
 
 #include "host.hpp"
-#include "tick.cuh"
+#include "kernels.cuh"
 
 using namespace epi;
+using namespace epi::kern;
 
-// ------------------------------------------------------------------ kernels
-namespace {
-
-constexpr int kThreads = 256;
-
-// Warp-aggregated 6-bin histogram into shared memory, then one atomic per bin per block.
-__device__ __forceinline__ void count_into(uint32_t* sh, bool valid, uint32_t bin) {
-    const int lane = threadIdx.x & 31;
-#pragma unroll
-    for (uint32_t b = 0; b < 6; ++b) {
-        uint32_t c = __popc(__ballot_sync(0xFFFFFFFFu, valid && bin == b));
-        if (lane == 0 && c) atomicAdd(&sh[b], c);
-    }
-}
-
-__device__ __forceinline__ void flush_counts(uint32_t* sh, uint32_t* row) {
-    __syncthreads();
-    if (threadIdx.x < 6 && sh[threadIdx.x]) atomicAdd(&row[threadIdx.x], sh[threadIdx.x]);
-}
-
-// Hours 1..6 (SLEEP_START_TIME..=SLEEP_END_TIME, citizen/mod.rs:244-248).
-__global__ void __launch_bounds__(kThreads) k_sleep(const DevParams* __restrict__ Pp, uint2* __restrict__ st,
-                                                    uint32_t* __restrict__ counts_row) {
-    __shared__ uint32_t sh[8];
-    if (threadIdx.x < 8) sh[threadIdx.x] = 0;
-    __syncthreads();
-    const uint32_t n = Pp->n;
-    const uint32_t stride = gridDim.x * blockDim.x;
-    for (uint32_t base = blockIdx.x * blockDim.x; base < n; base += stride) {
-        const uint32_t i = base + threadIdx.x;
-        const bool valid = i < n;
-        uint32_t s = 0;
-        if (valid) {
-            s = st[i].x;
-            if (st_ws(s) != EPI_WS_HOSPITAL_STAFF && st_area(s) != kHome) {
-                s = with_area(s, kHome);
-                st[i].x = s;
-            }
-        }
-        count_into(sh, valid, count_bin(s));
-    }
-    flush_counts(sh, counts_row);
-}
-
-// First vacant hospital cell of the snapshot in AreaIterator order (area.rs:221-237), found
-// by the whole block; kNoAction when the hospital is full.
-__device__ uint32_t block_first_vacant(const DevParams& P, const PlaneView& pl) {
-    __shared__ uint32_t best;
-    const Rect h = P.area[P.hosp_code];
-    const uint32_t w = (uint32_t)(h.x1 - h.x0 + 1), total = w * (uint32_t)(h.y1 - h.y0 + 1);
-    if (threadIdx.x == 0) best = kNoAction;
-    __syncthreads();
-    for (uint32_t base = 0; base < total; base += blockDim.x) {
-        const uint32_t c = base + threadIdx.x;
-        bool vac = false;
-        if (c < total) vac = pl.vacant(h.x0 + (int32_t)(c % w), h.y0 + (int32_t)(c / w));
-        if (vac) atomicMin(&best, c);
-        if (__syncthreads_or(vac)) break;
-    }
-    const uint32_t c = best;
-    __syncthreads();
-    if (c == kNoAction) return kNoAction;
-    return pack_xy(h.x0 + (int32_t)(c % w), h.y0 + (int32_t)(c / w));
-}
-
-// One hour of per-agent rules (hour of day 0, 7..22 or 23).
-__global__ void __launch_bounds__(kThreads) k_decide(const DevParams* __restrict__ Pp, const uint32_t* __restrict__ pos,
-                                                     uint2* __restrict__ st, const uint32_t* __restrict__ home,
-                                                     const uint32_t* __restrict__ work, uint32_t* __restrict__ wsa,
-                                                     const uint8_t* __restrict__ plane, uint32_t* __restrict__ claim,
-                                                     uint32_t* __restrict__ tgt, uint32_t* __restrict__ counts_row,
-                                                     const uint32_t* __restrict__ hour_base, uint32_t hour_offset,
-                                                     int* err) {
-    __shared__ uint32_t sh[8];
-    __shared__ DevParams sP;  // the parameter block, staged once per block
-    if (threadIdx.x < 8) sh[threadIdx.x] = 0;
-    for (uint32_t k = threadIdx.x; k < sizeof(DevParams) / 4; k += blockDim.x)
-        reinterpret_cast<uint32_t*>(&sP)[k] = reinterpret_cast<const uint32_t*>(Pp)[k];
-    __syncthreads();
-    const DevParams& P = sP;
-    const uint32_t hour = *hour_base + hour_offset;
-    const uint32_t hod = hour % 24u;
-    const PlaneView pl{plane, P.G, P.WP, err};
-    const uint32_t n = P.n;
-    const uint32_t stride = gridDim.x * blockDim.x;
-    uint32_t hosp_first = kNoAction;
-    bool hosp_known = false;
-    for (uint32_t base = blockIdx.x * blockDim.x; base < n; base += stride) {
-        const uint32_t i = base + threadIdx.x;
-        const bool valid = i < n;
-        uint32_t s = 0, at = 0, p = 0;
-        if (valid) {
-            const uint2 sv = st[i];
-            s = sv.x;
-            at = sv.y;
-            p = pos[i];
-        }
-        if (hod == 0u) {
-            const bool need = valid && wants_hospital(P, infected(s) ? with_day(s, st_day(s) + 1u) : s);
-            if (__syncthreads_or(need) && !hosp_known) {
-                hosp_first = block_first_vacant(P, pl);
-                hosp_known = true;
-            }
-        }
-        uint32_t bin = 0;
-        if (valid) {
-            const uint32_t s0 = s, at0 = at;
-            const uint32_t hm = home[i], wk = work[i];
-            const Cell cell{unpack_x(p), unpack_y(p)};
-            Draws dr{i, hour, P.key0, P.key1};
-            Cell nc;
-            if (hod == 0u) {
-                nc = routine_start(P, pl, s, hm, cell, hosp_first, dr);
-            } else if (hod == 23u) {
-                nc = routine_end(P, pl, s, hm, cell, dr);
-            } else {
-                const bool staff = st_ws(s) == EPI_WS_HOSPITAL_STAFF;
-                uint32_t w0 = staff ? wsa[i] : 0u, w = w0;
-                nc = perform_movements(P, pl, s, at, w, hm, wk, cell, hod, hour, dr);
-                if (staff && w != w0) wsa[i] = w;
-            }
-            bool moving = nc.x != cell.x || nc.y != cell.y;
-            if (moving && ((uint32_t)nc.x > (uint32_t)P.G || (uint32_t)nc.y > (uint32_t)P.G)) {
-                atomicOr(err, 4);  // unreachable for validated worlds; never write outside the plane
-                moving = false;
-                nc = cell;
-            }
-            const uint32_t cls = cell_class(P, s);
-            if (moving) atomicMin(&claim[(size_t)nc.y * P.W + nc.x], i);
-            tgt[i] = (moving || cls != cell_class(P, s0)) ? encode_target(nc, cls) : kNoAction;
-            if (s != s0 || at != at0) st[i] = make_uint2(s, at);
-            bin = count_bin(s);
-        }
-        count_into(sh, valid, bin);
-    }
-    flush_counts(sh, counts_row);
-}
-
-// Resolve the claims of the hour: the lowest index that claimed a cell moves there
-// (the serial resolve of allocation_map.rs:93-102 in index order), others keep their cell.
-__global__ void __launch_bounds__(kThreads) k_commit(const DevParams* __restrict__ Pp, uint32_t* __restrict__ pos,
-                                                     const uint32_t* __restrict__ tgt, uint8_t* __restrict__ plane,
-                                                     uint32_t* __restrict__ claim) {
-    const uint32_t n = Pp->n, W = (uint32_t)Pp->W, WP = (uint32_t)Pp->WP;
-    const uint32_t stride = gridDim.x * blockDim.x;
-    for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += stride) {
-        const uint32_t t = tgt[i];
-        if (t == kNoAction) continue;
-        const uint32_t p = pos[i];
-        const uint32_t xy = target_xy(t), cls = target_class(t);
-        const size_t old_cell = (size_t)(unpack_y(p) + 1) * WP + (unpack_x(p) + 1);
-        if (xy != p) {
-            const size_t claim_cell = (size_t)unpack_y(xy) * W + unpack_x(xy);
-            if (claim[claim_cell] == i) {
-                claim[claim_cell] = kNoClaim;
-                plane[old_cell] = 0;
-                plane[(size_t)(unpack_y(xy) + 1) * WP + (unpack_x(xy) + 1)] = (uint8_t)cls;
-                pos[i] = xy;
-                continue;
-            }
-        }
-        plane[old_cell] = (uint8_t)cls;
-    }
-}
-
-__global__ void k_build_plane(const DevParams* __restrict__ Pp, const uint32_t* __restrict__ pos,
-                              const uint2* __restrict__ st, uint8_t* __restrict__ plane, int* err) {
-    const uint32_t n = Pp->n;
-    const int32_t G = Pp->G, WP = Pp->WP;
-    for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
-        const uint32_t p = pos[i];
-        const int32_t x = unpack_x(p), y = unpack_y(p);
-        if (x > G || y > G) { atomicOr(err, 2); continue; }
-        plane[(size_t)(y + 1) * WP + (x + 1)] = (uint8_t)cell_class(*Pp, st[i].x);
-    }
-}
-
-// LockdownIntervention apply / revoke (allocation_map.rs:349-365).
-__global__ void k_lock(const DevParams* __restrict__ Pp, uint2* __restrict__ st, int on) {
-    const uint32_t n = Pp->n;
-    for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
-        uint32_t s = st[i].x;
-        uint32_t ns = on ? (st_ws(s) != EPI_WS_ESSENTIAL ? (s | kIso) : s) : (s & ~kIso);
-        if (ns != s) st[i].x = ns;
-    }
-}
-
-// vaccinate (allocation_map.rs:381-387): susceptible agents with Philox block 3 word 0 < thr.
-__global__ void k_vaccinate(const DevParams* __restrict__ Pp, uint2* __restrict__ st, uint32_t hour, uint64_t thr) {
-    const uint32_t n = Pp->n;
-    for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
-        uint32_t s = st[i].x;
-        if ((s & kStateMask) != EPI_S) continue;
-        uint32_t u[4];
-        philox4x32(i, hour, kBlkVaccine, 0u, Pp->key0, Pp->key1, u);
-        if ((uint64_t)u[0] < thr) st[i].x = s | kVacc;
-    }
-}
-
-// Invariants: each agent's cell holds its class; occupied cells == n; claims all free.
-__global__ void k_check_agents(const DevParams* __restrict__ Pp, const uint32_t* __restrict__ pos,
-                               const uint2* __restrict__ st, const uint8_t* __restrict__ plane,
-                               unsigned long long* bad) {
-    const uint32_t n = Pp->n;
-    const int32_t G = Pp->G, WP = Pp->WP;
-    for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
-        const uint32_t p = pos[i];
-        const int32_t x = unpack_x(p), y = unpack_y(p);
-        if (x > G || y > G || plane[(size_t)(y + 1) * WP + (x + 1)] != cell_class(*Pp, st[i].x)) atomicAdd(bad, 1ull);
-    }
-}
-
-__global__ void k_check_plane(size_t plane_bytes, const uint8_t* __restrict__ plane, size_t claim_cells,
-                              const uint32_t* __restrict__ claim, unsigned long long* occupied,
-                              unsigned long long* claimed) {
-    unsigned long long o = 0, c = 0;
-    const size_t stride = (size_t)gridDim.x * blockDim.x;
-    for (size_t k = blockIdx.x * (size_t)blockDim.x + threadIdx.x; k < plane_bytes; k += stride) o += plane[k] != 0;
-    for (size_t k = blockIdx.x * (size_t)blockDim.x + threadIdx.x; k < claim_cells; k += stride) c += claim[k] != kNoClaim;
-    for (int off = 16; off; off >>= 1) {
-        o += __shfl_down_sync(0xFFFFFFFFu, o, off);
-        c += __shfl_down_sync(0xFFFFFFFFu, c, off);
-    }
-    if ((threadIdx.x & 31) == 0) {
-        if (o) atomicAdd(occupied, o);
-        if (c) atomicAdd(claimed, c);
-    }
-}
-
-}  // namespace
-
-// ------------------------------------------------------------------ engine handle
 enum KernelKind { kKDecide = 0, kKCommit, kKSleep, kKLock, kKVaccinate, kKBuildPlane, kKCheck, kKindCount };
 static const char* kKernelNames[kKindCount] = {"k_decide", "k_commit", "k_sleep", "k_lock", "k_vaccinate", "k_build_plane", "k_check"};
 
-struct epi_engine {
+// One world on the device.
+struct Replica {
     epi_params p{};
     epi_geography geo0{}, geo{};
     DevParams hp{};
     uint32_t n = 0;
-    size_t plane_bytes = 0;  // padded byte plane (G+3)^2 + slack
-    size_t claim_cells = 0;  // (G+1)^2
-    int grid_blocks = 0;    // resident grid of the counting kernels (grid-stride loops)
-    int commit_blocks = 0;  // one thread per agent
+    InterventionState iv;
+    std::vector<epi_counts> rows;
+    bool active = true;
+    // checkpoint of the host-side state (epi_engine_save_state)
+    InterventionState s_iv;
+    epi_geography s_geo{};
+    uint32_t s_hosp_code = kHosp0;
+    bool s_active = true;
+};
+
+struct epi_engine {
+    std::vector<Replica> reps;
+    uint32_t slots = 0;        // agent slots (chunk-padded replicates)
+    size_t plane_bytes = 0;    // all bordered byte planes
+    size_t claim_cells = 0;    // all claim planes
+    int grid_blocks = 0;       // resident grid of the counting kernels
+    int commit_blocks = 0;     // one thread per slot
     // device
     DevParams* d_params = nullptr;
+    uint32_t* d_chunk_rep = nullptr;  // null for a single replicate
     uint32_t *d_pos = nullptr, *d_home = nullptr, *d_work = nullptr, *d_wsa = nullptr, *d_tgt = nullptr;
     uint2* d_st = nullptr;
     uint8_t* d_plane = nullptr;
     uint32_t* d_claim = nullptr;
-    uint32_t* d_counts = nullptr;
+    uint32_t* d_counts = nullptr;  // [hour of segment][replicate][8]
     uint32_t* d_hour_base = nullptr;
     int* d_err = nullptr;
     unsigned long long* d_scratch = nullptr;
-    uint32_t counts_capacity = 0;
+    uint32_t counts_capacity = 0;  // hours
     // host
-    uint32_t* h_counts = nullptr;  // pinned
+    uint32_t* h_counts = nullptr;  // pinned mirror of d_counts
     uint32_t* h_hour_base = nullptr;
     cudaStream_t stream = nullptr;
     bool own_stream = false;
     std::map<std::pair<uint32_t, uint32_t>, cudaGraphExec_t> graphs;  // (first hour mod 24, hours)
-    InterventionState iv;
-    std::vector<epi_counts> rows;
     std::string err;
     bool profiling = false;
     uint32_t launches[kKindCount] = {};
@@ -294,14 +76,17 @@ struct epi_engine {
     std::vector<std::pair<int, std::pair<cudaEvent_t, cudaEvent_t>>> pending;
     std::vector<cudaEvent_t> event_pool;
     uint64_t kernels_launched = 0;
-    // device-side checkpoint (epi_engine_save_state / epi_engine_restore_state)
+    // device-side checkpoint
     uint32_t *s_pos = nullptr, *s_wsa = nullptr;
     uint2* s_st = nullptr;
     uint8_t* s_plane = nullptr;
     bool saved = false;
-    InterventionState s_iv;
-    uint32_t s_hosp_code = kHosp0;
-    epi_geography s_geo{};
+
+    uint32_t R() const { return (uint32_t)reps.size(); }
+};
+
+struct epi_ensemble {
+    epi_engine core;
 };
 
 static thread_local std::string g_create_error;
@@ -315,32 +100,21 @@ static thread_local std::string g_create_error;
         }                                                                                    \
     } while (0)
 
-static uint32_t area_code_of(const epi_engine* h, const epi_agent_record& r, bool* ok) {
-    Rect a{r.area_x0, r.area_y0, r.area_x1, r.area_y1};
-    *ok = true;
-    if (rect_eq(a, Rect{r.home_x, r.home_y, r.home_x + 1, r.home_y + 1})) return kHome;
-    if (r.work_status != EPI_WS_NA && rect_eq(a, Rect{r.work_x, r.work_y, r.work_x + 9, r.work_y + 9})) return kWork;
-    for (uint32_t c = kTransport; c < kNumAreas; ++c)
-        if (rect_eq(a, h->hp.area[c])) return c;
-    *ok = false;
-    return kHome;
-}
-
 static Rect to_rect(const epi_area& a) { return Rect{a.x0, a.y0, a.x1, a.y1}; }
 
-static void fill_dev_params(epi_engine* h) {
-    DevParams& d = h->hp;
+// Device parameters of one world: areas, random key, disease thresholds.
+static DevParams make_dev_params(const epi_params& p, const epi_geography& geo0, uint32_t n) {
+    DevParams d;
     std::memset(&d, 0, sizeof d);
-    const epi_params& p = h->p;
-    d.n = h->n;
+    d.n = n;
     d.G = (int32_t)p.grid_size;
     d.W = d.G + 1;
     d.WP = d.G + 3;
     d.hosp_code = kHosp0;
-    d.area[kTransport] = to_rect(h->geo0.transport);
-    d.area[kHousing] = to_rect(h->geo0.housing);
-    d.area[kHosp0] = to_rect(h->geo0.hospital);
-    d.area[kHosp1] = to_rect(grown_hospital(h->geo0));
+    d.area[kTransport] = to_rect(geo0.transport);
+    d.area[kHousing] = to_rect(geo0.housing);
+    d.area[kHosp0] = to_rect(geo0.hospital);
+    d.area[kHosp1] = to_rect(grown_hospital(geo0));
     d.key0 = (uint32_t)p.seed;
     d.key1 = (uint32_t)(p.seed >> 32);
     d.reg_start = p.regular_transmission_start_day;
@@ -349,7 +123,6 @@ static void fill_dev_params(epi_engine* h) {
     d.exposed_duration = p.exposed_duration;
     d.pre_duration = p.pre_symptomatic_duration;
     const double rates[3] = {0.0, p.regular_transmission_rate, p.high_transmission_rate};
-    d.hosp_if_class = 0;
     for (int c = 0; c < 3; ++c) {
         d.thr_rate[c] = bernoulli_threshold(rates[c]);
         if (rates[c] >= p.high_transmission_rate) d.hosp_if_class |= 1u << c;  // is_to_be_hospitalized
@@ -357,8 +130,22 @@ static void fill_dev_params(epi_engine* h) {
     d.thr_death = bernoulli_threshold(p.death_rate);
     d.thr_symptoms = bernoulli_threshold(1.0 - p.percentage_asymptomatic_population);
     d.thr_severe = bernoulli_threshold(p.percentage_severe_infected_population);
+    d.active = 1;
+    return d;
 }
 
+static uint32_t area_code_of(const DevParams& hp, const epi_agent_record& r, bool* ok) {
+    Rect a{r.area_x0, r.area_y0, r.area_x1, r.area_y1};
+    *ok = true;
+    if (rect_eq(a, Rect{r.home_x, r.home_y, r.home_x + 1, r.home_y + 1})) return kHome;
+    if (r.work_status != EPI_WS_NA && rect_eq(a, Rect{r.work_x, r.work_y, r.work_x + 9, r.work_y + 9})) return kWork;
+    for (uint32_t c = kTransport; c < kNumAreas; ++c)
+        if (rect_eq(a, hp.area[c])) return c;
+    *ok = false;
+    return kHome;
+}
+
+// ------------------------------------------------------------------ launch bookkeeping
 static int record_launch_begin(epi_engine* h, int kind, cudaEvent_t* out_end) {
     if (!h->profiling) return EPI_OK;
     cudaEvent_t a, b;
@@ -405,40 +192,53 @@ static int harvest_events(epi_engine* h) {
         if (rc_) return rc_;                                                                 \
     } while (0)
 
-static int ensure_counts(epi_engine* h, uint32_t rows_needed) {
-    if (rows_needed <= h->counts_capacity) return EPI_OK;
-    uint32_t cap = std::max<uint32_t>(rows_needed, 64);
+static int push_params(epi_engine* h) {
+    std::vector<DevParams> all(h->R());
+    for (uint32_t r = 0; r < h->R(); ++r) all[r] = h->reps[r].hp;
+    CK(cudaMemcpyAsync(h->d_params, all.data(), all.size() * sizeof(DevParams), cudaMemcpyHostToDevice, h->stream));
+    CK(cudaStreamSynchronize(h->stream));
+    return EPI_OK;
+}
+
+static int ensure_counts(epi_engine* h, uint32_t hours_needed) {
+    if (hours_needed <= h->counts_capacity) return EPI_OK;
+    uint32_t cap = std::max<uint32_t>(hours_needed, 48);
     if (h->d_counts) CK(cudaFree(h->d_counts));
     if (h->h_counts) CK(cudaFreeHost(h->h_counts));
     h->d_counts = nullptr;
     h->h_counts = nullptr;
-    CK(cudaMalloc(&h->d_counts, (size_t)cap * 8 * sizeof(uint32_t)));
-    CK(cudaMallocHost(&h->h_counts, (size_t)cap * 8 * sizeof(uint32_t)));
+    const size_t words = (size_t)cap * h->R() * 8;
+    CK(cudaMalloc(&h->d_counts, words * sizeof(uint32_t)));
+    CK(cudaMallocHost(&h->h_counts, words * sizeof(uint32_t)));
     h->counts_capacity = cap;
-    // cached graphs reference the old counts buffer
-    for (auto& g : h->graphs) cudaGraphExecDestroy(g.second);
+    for (auto& g : h->graphs) cudaGraphExecDestroy(g.second);  // they reference the old buffer
     h->graphs.clear();
     return EPI_OK;
 }
 
-// Issue the kernels of hours hour_base .. hour_base + n - 1 (hour_base read on the device).
+// ------------------------------------------------------------------ the hour loop
+// Kernels of hours hour_base .. hour_base + nh - 1 (hour_base read on the device).
 static int enqueue_hours(epi_engine* h, uint32_t first_hour, uint32_t nh) {
-    CK(cudaMemsetAsync(h->d_counts, 0, (size_t)nh * 8 * sizeof(uint32_t), h->stream));
-    const int blocks = h->grid_blocks;
+    const size_t row_words = (size_t)h->R() * 8;
+    CK(cudaMemsetAsync(h->d_counts, 0, (size_t)nh * row_words * sizeof(uint32_t), h->stream));
+    const uint32_t n_chunks = h->slots / kChunk;
     for (uint32_t k = 0; k < nh; ++k) {
         const uint32_t hod = (first_hour + k) % 24u;
-        uint32_t* row = h->d_counts + (size_t)k * 8;
+        uint32_t* rows = h->d_counts + (size_t)k * row_words;
         if (hod >= 1u && hod <= 6u) {
-            LAUNCH(kKSleep, (k_sleep<<<blocks, kThreads, 0, h->stream>>>(h->d_params, h->d_st, row)));
+            LAUNCH(kKSleep, (k_sleep<<<h->grid_blocks, kThreads, 0, h->stream>>>(h->d_params, h->d_chunk_rep, n_chunks,
+                                                                                  h->d_st, rows)));
         } else {
-            LAUNCH(kKDecide, (k_decide<<<blocks, kThreads, 0, h->stream>>>(
-                                  h->d_params, h->d_pos, h->d_st, h->d_home, h->d_work, h->d_wsa, h->d_plane, h->d_claim,
-                                  h->d_tgt, row, h->d_hour_base, k, h->d_err)));
-            LAUNCH(kKCommit, (k_commit<<<h->commit_blocks, kThreads, 0, h->stream>>>(h->d_params, h->d_pos, h->d_tgt, h->d_plane,
-                                                                           h->d_claim)));
+            LAUNCH(kKDecide, (k_decide<<<h->grid_blocks, kThreads, 0, h->stream>>>(
+                                  h->d_params, h->d_chunk_rep, n_chunks, h->d_pos, h->d_st, h->d_home, h->d_work, h->d_wsa,
+                                  h->d_plane, h->d_claim, h->d_tgt, rows, h->d_hour_base, k, h->d_err)));
+            LAUNCH(kKCommit, (k_commit<<<h->commit_blocks, kThreads, 0, h->stream>>>(h->d_params, h->d_chunk_rep, h->slots,
+                                                                                     h->d_pos, h->d_tgt, h->d_plane,
+                                                                                     h->d_claim)));
         }
     }
-    CK(cudaMemcpyAsync(h->h_counts, h->d_counts, (size_t)nh * 8 * sizeof(uint32_t), cudaMemcpyDeviceToHost, h->stream));
+    CK(cudaMemcpyAsync(h->h_counts, h->d_counts, (size_t)nh * row_words * sizeof(uint32_t), cudaMemcpyDeviceToHost,
+                       h->stream));
     return EPI_OK;
 }
 
@@ -453,7 +253,9 @@ static int check_error_flag(epi_engine* h) {
     return EPI_OK;
 }
 
-static int run_hours(epi_engine* h, uint32_t first_hour, uint32_t nh, epi_counts* out) {
+// Simulate hours first_hour .. first_hour + nh - 1 for every active replicate; the counts
+// of hour k of replicate r land in h_counts[(k * R + r) * 8 ..].
+static int run_hours(epi_engine* h, uint32_t first_hour, uint32_t nh) {
     if (nh == 0) return EPI_OK;
     if ((uint64_t)first_hour + nh > 0xFFFFFFFFull) { h->err = "hour out of range"; return EPI_ERR_ARG; }
     int rc = ensure_counts(h, nh);
@@ -491,30 +293,164 @@ static int run_hours(epi_engine* h, uint32_t first_hour, uint32_t nh, epi_counts
     rc = check_error_flag(h);
     if (rc) return rc;
     for (uint32_t k = 0; k < nh; ++k) {
-        const uint32_t* c = h->h_counts + (size_t)k * 8;
-        epi_counts& o = out[k];
-        o.hour = first_hour + k;
-        o.susceptible = c[0];
-        o.exposed = c[1];
-        o.infected = c[2];
-        o.hospitalized = c[3];
-        o.recovered = c[4];
-        o.deceased = c[5];
-        uint64_t total = (uint64_t)c[0] + c[1] + c[2] + c[3] + c[4] + c[5];
-        if (total != h->n) {  // assert_eq!(csv_record.total(), current_population), allocation_map.rs:128
-            h->err = "counts total " + std::to_string(total) + " != population " + std::to_string(h->n);
-            return EPI_ERR_INVARIANT;
+        for (uint32_t r = 0; r < h->R(); ++r) {
+            if (!h->reps[r].active) continue;
+            const uint32_t* c = h->h_counts + ((size_t)k * h->R() + r) * 8;
+            const uint64_t total = (uint64_t)c[0] + c[1] + c[2] + c[3] + c[4] + c[5];
+            if (total != h->reps[r].n) {  // assert_eq!(csv_record.total(), current_population), allocation_map.rs:128
+                h->err = "replicate " + std::to_string(r) + ": counts total " + std::to_string(total) + " != population " +
+                         std::to_string(h->reps[r].n);
+                return EPI_ERR_INVARIANT;
+            }
         }
     }
     return EPI_OK;
 }
 
+static epi_counts counts_of(const epi_engine* h, uint32_t k, uint32_t r, uint32_t hour) {
+    const uint32_t* c = h->h_counts + ((size_t)k * h->R() + r) * 8;
+    epi_counts o;
+    o.hour = hour;
+    o.susceptible = c[0];
+    o.exposed = c[1];
+    o.infected = c[2];
+    o.hospitalized = c[3];
+    o.recovered = c[4];
+    o.deceased = c[5];
+    return o;
+}
+
+// ------------------------------------------------------------------ interventions
+static int bulk_done(epi_engine* h) {
+    CK(cudaStreamSynchronize(h->stream));
+    h->kernels_launched += 1;
+    return harvest_events(h);
+}
+
+static int blocks_for(uint32_t n) { return (int)std::max<uint32_t>(1u, std::min<uint32_t>((n + kThreads - 1) / kThreads, 4096u)); }
+
+static int lock_city(epi_engine* h, uint32_t r, int on) {
+    const Replica& rep = h->reps[r];
+    LAUNCH(kKLock, (k_lock<<<blocks_for(rep.n), kThreads, 0, h->stream>>>(h->d_st, rep.hp.agent_off, rep.n, on)));
+    return bulk_done(h);
+}
+
+static int vaccinate(epi_engine* h, uint32_t r, uint32_t hour, double percent) {
+    const Replica& rep = h->reps[r];
+    const uint64_t thr = bernoulli_threshold(percent);
+    LAUNCH(kKVaccinate, (k_vaccinate<<<blocks_for(rep.n), kThreads, 0, h->stream>>>(h->d_st, rep.hp.agent_off, rep.n,
+                                                                                    rep.hp.key0, rep.hp.key1, hour, thr)));
+    return bulk_done(h);
+}
+
+static void grow_hospital(epi_engine* h, uint32_t r) {
+    Replica& rep = h->reps[r];
+    const epi_area grown = grown_hospital(rep.geo0);
+    rep.geo.hospital = grown;
+    rep.hp.hosp_code = rect_eq(to_rect(grown), rep.hp.area[kHosp0]) ? kHosp0 : kHosp1;
+}
+
+// process_interventions of one replicate; returns EPI_IV_* bits in *applied.  Parameter
+// changes (hospital) are left for the caller to push.
+static int process_interventions(epi_engine* h, uint32_t r, const epi_counts& c, uint32_t* applied, bool* params_dirty) {
+    Replica& rep = h->reps[r];
+    InterventionActions a = decide_interventions(rep.p, rep.iv, c, rep.geo.hospital);
+    int rc = EPI_OK;
+    if (a.vaccinate && (rc = vaccinate(h, r, c.hour, a.vaccinate_percent))) return rc;
+    if (a.lock && (rc = lock_city(h, r, 1))) return rc;
+    if (a.unlock && (rc = lock_city(h, r, 0))) return rc;
+    if (a.grow_hospital) {
+        grow_hospital(h, r);
+        *params_dirty = true;
+    }
+    if (applied) *applied = a.applied;
+    return EPI_OK;
+}
+
+// run_single_engine for every replicate in lockstep: segments end at any replicate's
+// intervention point or final hour; after each segment every active replicate takes its
+// rows, its interventions and its stop rule (epidemiology_simulation.rs:223-269, 564-575).
+static int set_all_active(epi_engine* h) {
+    for (auto& rep : h->reps) {
+        rep.active = true;
+        rep.hp.active = 1;
+    }
+    return push_params(h);
+}
+
+static int run_loop_body(epi_engine* h);
+
+// Replicates drop out of the lockstep loop as their runs end; afterwards all of them are
+// active again, so that direct hour calls keep working on every world.
+static int run_loop(epi_engine* h) {
+    int rc = run_loop_body(h);
+    int rc2 = set_all_active(h);
+    return rc ? rc : rc2;
+}
+
+static int run_loop_body(epi_engine* h) {
+    uint32_t last = 0;  // last simulated hour over all replicates
+    for (auto& rep : h->reps) {
+        rep.rows.clear();
+        rep.active = rep.p.hours >= 2;
+        rep.hp.active = rep.active ? 1u : 0u;
+        if (rep.active) last = std::max(last, rep.p.hours - 1);
+    }
+    uint32_t hour = 1;
+    bool dirty = true;
+    while (hour <= last) {
+        bool any = false;
+        for (auto& rep : h->reps) any |= rep.active;
+        if (!any) break;
+        if (dirty) {
+            int rc = push_params(h);
+            if (rc) return rc;
+            dirty = false;
+        }
+        uint32_t end = hour;
+        for (;; ++end) {
+            if (end >= last) break;
+            bool boundary = false;
+            for (const auto& rep : h->reps)
+                if (rep.active && (is_event_hour(rep.p, end) || end + 1 == rep.p.hours)) boundary = true;
+            if (boundary) break;
+        }
+        const uint32_t nh = end - hour + 1;
+        int rc = run_hours(h, hour, nh);
+        if (rc) return rc;
+        for (uint32_t r = 0; r < h->R(); ++r) {
+            Replica& rep = h->reps[r];
+            if (!rep.active) continue;
+            for (uint32_t k = 0; k < nh; ++k) {
+                const uint32_t hr = hour + k;
+                const epi_counts c = counts_of(h, k, r, hr);
+                rep.rows.push_back(c);
+                if (k + 1 == nh) {  // interventions only fire at intervention points, which end segments
+                    rc = process_interventions(h, r, c, nullptr, &dirty);
+                    if (rc) return rc;
+                }
+                const bool stop = c.exposed == 0 && c.infected == 0 && c.hospitalized == 0;
+                if (stop || hr + 1 >= rep.p.hours) {
+                    rep.active = false;
+                    rep.hp.active = 0;
+                    dirty = true;
+                    break;
+                }
+            }
+        }
+        hour = end + 1;
+    }
+    if (dirty) return push_params(h);
+    return EPI_OK;
+}
+
+// ------------------------------------------------------------------ create / destroy
 static void free_device(epi_engine* h) {
     for (auto& g : h->graphs) cudaGraphExecDestroy(g.second);
     h->graphs.clear();
-    cudaFree(h->d_params); cudaFree(h->d_pos); cudaFree(h->d_home); cudaFree(h->d_work); cudaFree(h->d_wsa);
-    cudaFree(h->d_tgt); cudaFree(h->d_st); cudaFree(h->d_plane); cudaFree(h->d_claim); cudaFree(h->d_counts);
-    cudaFree(h->d_hour_base); cudaFree(h->d_err); cudaFree(h->d_scratch);
+    cudaFree(h->d_params); cudaFree(h->d_chunk_rep); cudaFree(h->d_pos); cudaFree(h->d_home); cudaFree(h->d_work);
+    cudaFree(h->d_wsa); cudaFree(h->d_tgt); cudaFree(h->d_st); cudaFree(h->d_plane); cudaFree(h->d_claim);
+    cudaFree(h->d_counts); cudaFree(h->d_hour_base); cudaFree(h->d_err); cudaFree(h->d_scratch);
     cudaFree(h->s_pos); cudaFree(h->s_wsa); cudaFree(h->s_st); cudaFree(h->s_plane);
     if (h->h_counts) cudaFreeHost(h->h_counts);
     if (h->h_hour_base) cudaFreeHost(h->h_hour_base);
@@ -523,114 +459,291 @@ static void free_device(epi_engine* h) {
     if (h->own_stream && h->stream) cudaStreamDestroy(h->stream);
 }
 
-static int upload_world(epi_engine* h, const epi_agent_record* recs) {
-    const uint32_t n = h->n;
-    std::vector<uint32_t> pos(n), home(n), work(n), wsa(n);
-    std::vector<uint2> st(n);
-    for (uint32_t i = 0; i < n; ++i) {
-        const epi_agent_record& r = recs[i];
-        const int32_t G = (int32_t)h->p.grid_size;
-        auto inside = [G](int32_t x0, int32_t y0, int32_t x1, int32_t y1) {
-            return x0 >= 0 && y0 >= 0 && x1 <= G && y1 <= G && x0 <= x1 && y0 <= y1;
-        };
-        if (r.x < 0 || r.y < 0 || r.x > G || r.y > G || r.state > EPI_D || r.work_status > EPI_WS_NA ||
-            r.immunity < -2 || r.immunity > 2 || r.infection_day > 0xFFFFu ||
-            !inside(r.home_x, r.home_y, r.home_x + 1, r.home_y + 1) ||
-            (r.work_status != EPI_WS_NA && !inside(r.work_x, r.work_y, r.work_x + 9, r.work_y + 9)) ||
-            !inside(r.area_x0, r.area_y0, r.area_x1, r.area_y1)) {
-            h->err = "agent record " + std::to_string(i) + " out of range";
+static size_t align_up(size_t v, size_t a) { return (v + a - 1) / a * a; }
+
+// Pack one replicate's records into the host mirrors of the SoA arrays.
+static int pack_replica(const epi_engine* h, uint32_t r, const epi_agent_record* recs, uint32_t* pos, uint2* st,
+                        uint32_t* home, uint32_t* work, uint32_t* wsa, std::string& err) {
+    const Replica& rep = h->reps[r];
+    const int32_t G = (int32_t)rep.p.grid_size;
+    auto inside = [G](int32_t x0, int32_t y0, int32_t x1, int32_t y1) {
+        return x0 >= 0 && y0 >= 0 && x1 <= G && y1 <= G && x0 <= x1 && y0 <= y1;
+    };
+    for (uint32_t i = 0; i < rep.n; ++i) {
+        const epi_agent_record& a = recs[i];
+        if (a.x < 0 || a.y < 0 || a.x > G || a.y > G || a.state > EPI_D || a.work_status > EPI_WS_NA ||
+            a.immunity < -2 || a.immunity > 2 || a.infection_day > 0xFFFFu ||
+            !inside(a.home_x, a.home_y, a.home_x + 1, a.home_y + 1) ||
+            (a.work_status != EPI_WS_NA && !inside(a.work_x, a.work_y, a.work_x + 9, a.work_y + 9)) ||
+            !inside(a.area_x0, a.area_y0, a.area_x1, a.area_y1)) {
+            err = "replicate " + std::to_string(r) + ": agent record " + std::to_string(i) + " out of range";
             return EPI_ERR_ARG;
         }
         bool ok = true;
-        uint32_t code = area_code_of(h, r, &ok);
-        if (!ok) { h->err = "agent record " + std::to_string(i) + ": current area is not one of its areas"; return EPI_ERR_ARG; }
-        uint32_t s = (uint32_t)r.state;
-        if (r.flags & EPI_F_HOSPITALIZED) s |= kHosp;
-        if (r.flags & EPI_F_ISOLATED) s |= kIso;
-        if (r.flags & EPI_F_VACCINATED) s |= kVacc;
-        if (r.flags & EPI_F_WORK_QUARANTINED) s |= kWq;
-        if (r.flags & EPI_F_PUBLIC_TRANSPORT) s |= kPt;
+        const uint32_t code = area_code_of(rep.hp, a, &ok);
+        if (!ok) {
+            err = "replicate " + std::to_string(r) + ": agent record " + std::to_string(i) +
+                  ": current area is not one of its areas";
+            return EPI_ERR_ARG;
+        }
+        uint32_t s = (uint32_t)a.state;
+        if (a.flags & EPI_F_HOSPITALIZED) s |= kHosp;
+        if (a.flags & EPI_F_ISOLATED) s |= kIso;
+        if (a.flags & EPI_F_VACCINATED) s |= kVacc;
+        if (a.flags & EPI_F_WORK_QUARANTINED) s |= kWq;
+        if (a.flags & EPI_F_PUBLIC_TRANSPORT) s |= kPt;
         s |= code << kAreaShift;
-        s |= (uint32_t)r.work_status << kWsShift;
-        s |= (uint32_t)(r.immunity + 2) << kImmShift;
-        s |= r.infection_day << kDayShift;
-        st[i] = make_uint2(s, r.at_hour);
-        pos[i] = pack_xy(r.x, r.y);
-        home[i] = pack_xy(r.home_x, r.home_y);
-        work[i] = pack_xy(r.work_x, r.work_y);
-        wsa[i] = r.work_start_at;
+        s |= (uint32_t)a.work_status << kWsShift;
+        s |= (uint32_t)(a.immunity + 2) << kImmShift;
+        s |= a.infection_day << kDayShift;
+        const size_t slot = rep.hp.agent_off + i;
+        st[slot] = make_uint2(s, a.at_hour);
+        pos[slot] = pack_xy(a.x, a.y);
+        home[slot] = pack_xy(a.home_x, a.home_y);
+        work[slot] = pack_xy(a.work_x, a.work_y);
+        wsa[slot] = a.work_start_at;
     }
-    CK(cudaMemcpyAsync(h->d_pos, pos.data(), n * sizeof(uint32_t), cudaMemcpyHostToDevice, h->stream));
-    CK(cudaMemcpyAsync(h->d_home, home.data(), n * sizeof(uint32_t), cudaMemcpyHostToDevice, h->stream));
-    CK(cudaMemcpyAsync(h->d_work, work.data(), n * sizeof(uint32_t), cudaMemcpyHostToDevice, h->stream));
-    CK(cudaMemcpyAsync(h->d_wsa, wsa.data(), n * sizeof(uint32_t), cudaMemcpyHostToDevice, h->stream));
-    CK(cudaMemcpyAsync(h->d_st, st.data(), n * sizeof(uint2), cudaMemcpyHostToDevice, h->stream));
-    CK(cudaMemsetAsync(h->d_plane, 0, h->plane_bytes, h->stream));
-    CK(cudaMemsetAsync(h->d_claim, 0xFF, h->claim_cells * sizeof(uint32_t), h->stream));
-    CK(cudaMemsetAsync(h->d_err, 0, sizeof(int), h->stream));
-    LAUNCH(kKBuildPlane, (k_build_plane<<<h->grid_blocks, kThreads, 0, h->stream>>>(h->d_params, h->d_pos, h->d_st,
-                                                                                      h->d_plane, h->d_err)));
-    CK(cudaStreamSynchronize(h->stream));  // host vectors go out of scope
-    int rc = harvest_events(h);
-    if (rc) return rc;
-    return check_error_flag(h);
+    return EPI_OK;
 }
 
-static int engine_init(epi_engine* h, const epi_params& p, const epi_agent_record* recs, size_t n) {
-    h->p = p;
-    std::string bad = validate_params(p);
-    if (!bad.empty()) { h->err = bad; return EPI_ERR_CONFIG; }
-    if (n != p.number_of_agents || n == 0 || n >= 0xFFFFFFFFull) { h->err = "record count != number_of_agents"; return EPI_ERR_ARG; }
-    h->n = (uint32_t)n;
-    h->geo0 = define_geography(p.grid_size);
-    resize_hospital(h->geo0, (int32_t)n, 0.002, p.hospital_beds_percentage);
-    h->geo = h->geo0;
-    fill_dev_params(h);
-    const size_t W = (size_t)p.grid_size + 1;
-    h->claim_cells = W * W;
-    h->plane_bytes = (W + 2) * (W + 2) + 16;  // border of one cell, 16 B slack for the row loads
+// Lay out and upload R worlds given as per-replicate record arrays.
+static int engine_init(epi_engine* h, const epi_params* params, const epi_agent_record* const* recs, uint32_t R) {
+    if (R == 0) { h->err = "no replicates"; return EPI_ERR_ARG; }
+    h->reps.resize(R);
+    uint64_t slots = 0, plane = 0, claim = 0;
+    for (uint32_t r = 0; r < R; ++r) {
+        Replica& rep = h->reps[r];
+        rep.p = params[r];
+        const std::string bad = validate_params(rep.p);
+        if (!bad.empty()) { h->err = "replicate " + std::to_string(r) + ": " + bad; return EPI_ERR_CONFIG; }
+        rep.n = rep.p.number_of_agents;
+        rep.geo0 = define_geography(rep.p.grid_size);
+        resize_hospital(rep.geo0, (int32_t)rep.n, 0.002, rep.p.hospital_beds_percentage);
+        rep.geo = rep.geo0;
+        rep.hp = make_dev_params(rep.p, rep.geo0, rep.n);
+        rep.hp.agent_off = (uint32_t)slots;
+        rep.hp.plane_off = plane;
+        rep.hp.claim_off = claim;
+        const uint64_t side = (uint64_t)rep.p.grid_size + 1;
+        slots += align_up(rep.n, kChunk);
+        plane += align_up((side + 2) * (side + 2) + 16, 256);
+        claim += side * side;
+        if (slots >= 0xFFFFFFFFull - kChunk) { h->err = "too many agents for one engine"; return EPI_ERR_CAPACITY; }
+    }
+    h->slots = (uint32_t)slots;
+    h->plane_bytes = plane;
+    h->claim_cells = claim;
     int dev = 0, sms = 0, per_sm = 0;
     CK(cudaGetDevice(&dev));
     CK(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev));
     CK(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_decide, kThreads, 0));
     per_sm = std::max(per_sm, 1);
-    const uint64_t need_blocks = ((uint64_t)n + kThreads - 1) / kThreads;
-    h->grid_blocks = (int)std::min<uint64_t>(need_blocks, (uint64_t)sms * per_sm);
-    h->commit_blocks = (int)need_blocks;
+    const uint64_t n_chunks = slots / kChunk;
+    h->grid_blocks = (int)std::min<uint64_t>(n_chunks, (uint64_t)sms * per_sm);
+    h->commit_blocks = (int)n_chunks;
     CK(cudaStreamCreateWithFlags(&h->stream, cudaStreamNonBlocking));
     h->own_stream = true;
-    CK(cudaMalloc(&h->d_params, sizeof(DevParams)));
-    CK(cudaMalloc(&h->d_pos, n * sizeof(uint32_t)));
-    CK(cudaMalloc(&h->d_home, n * sizeof(uint32_t)));
-    CK(cudaMalloc(&h->d_work, n * sizeof(uint32_t)));
-    CK(cudaMalloc(&h->d_wsa, n * sizeof(uint32_t)));
-    CK(cudaMalloc(&h->d_tgt, n * sizeof(uint32_t)));
-    CK(cudaMalloc(&h->d_st, n * sizeof(uint2)));
+    CK(cudaMalloc(&h->d_params, R * sizeof(DevParams)));
+    if (R > 1) {
+        std::vector<uint32_t> chunk_rep(n_chunks);
+        for (uint32_t r = 0; r < R; ++r) {
+            const uint64_t c0 = h->reps[r].hp.agent_off / kChunk, c1 = c0 + align_up(h->reps[r].n, kChunk) / kChunk;
+            for (uint64_t c = c0; c < c1; ++c) chunk_rep[c] = r;
+        }
+        CK(cudaMalloc(&h->d_chunk_rep, n_chunks * sizeof(uint32_t)));
+        CK(cudaMemcpyAsync(h->d_chunk_rep, chunk_rep.data(), n_chunks * sizeof(uint32_t), cudaMemcpyHostToDevice, h->stream));
+        CK(cudaStreamSynchronize(h->stream));
+    }
+    CK(cudaMalloc(&h->d_pos, slots * sizeof(uint32_t)));
+    CK(cudaMalloc(&h->d_home, slots * sizeof(uint32_t)));
+    CK(cudaMalloc(&h->d_work, slots * sizeof(uint32_t)));
+    CK(cudaMalloc(&h->d_wsa, slots * sizeof(uint32_t)));
+    CK(cudaMalloc(&h->d_tgt, slots * sizeof(uint32_t)));
+    CK(cudaMalloc(&h->d_st, slots * sizeof(uint2)));
     CK(cudaMalloc(&h->d_plane, h->plane_bytes));
     CK(cudaMalloc(&h->d_claim, h->claim_cells * sizeof(uint32_t)));
     CK(cudaMalloc(&h->d_hour_base, sizeof(uint32_t)));
     CK(cudaMalloc(&h->d_err, sizeof(int)));
     CK(cudaMalloc(&h->d_scratch, 4 * sizeof(unsigned long long)));
     CK(cudaMallocHost(&h->h_hour_base, sizeof(uint32_t)));
-    CK(cudaMemcpyAsync(h->d_params, &h->hp, sizeof(DevParams), cudaMemcpyHostToDevice, h->stream));
     int rc = ensure_counts(h, 48);
     if (rc) return rc;
-    return upload_world(h, recs);
+    // host mirrors, filled per replicate (in parallel for large ensembles)
+    std::vector<uint32_t> pos(slots, 0), home(slots, 0), work(slots, 0), wsa(slots, 0);
+    std::vector<uint2> st(slots, make_uint2(0, 0));
+    std::vector<int> status(R, EPI_OK);
+    std::vector<std::string> errs(R);
+    const unsigned workers = std::max(1u, std::min<unsigned>(R, std::thread::hardware_concurrency()));
+    std::vector<std::thread> pool;
+    for (unsigned w = 0; w < workers; ++w)
+        pool.emplace_back([&, w] {
+            for (uint32_t r = w; r < R; r += workers)
+                status[r] = pack_replica(h, r, recs[r], pos.data(), st.data(), home.data(), work.data(), wsa.data(), errs[r]);
+        });
+    for (auto& t : pool) t.join();
+    for (uint32_t r = 0; r < R; ++r)
+        if (status[r]) { h->err = errs[r]; return status[r]; }
+    CK(cudaMemcpyAsync(h->d_pos, pos.data(), slots * sizeof(uint32_t), cudaMemcpyHostToDevice, h->stream));
+    CK(cudaMemcpyAsync(h->d_home, home.data(), slots * sizeof(uint32_t), cudaMemcpyHostToDevice, h->stream));
+    CK(cudaMemcpyAsync(h->d_work, work.data(), slots * sizeof(uint32_t), cudaMemcpyHostToDevice, h->stream));
+    CK(cudaMemcpyAsync(h->d_wsa, wsa.data(), slots * sizeof(uint32_t), cudaMemcpyHostToDevice, h->stream));
+    CK(cudaMemcpyAsync(h->d_st, st.data(), slots * sizeof(uint2), cudaMemcpyHostToDevice, h->stream));
+    CK(cudaMemsetAsync(h->d_tgt, 0xFF, slots * sizeof(uint32_t), h->stream));
+    CK(cudaMemsetAsync(h->d_plane, 0, h->plane_bytes, h->stream));
+    CK(cudaMemsetAsync(h->d_claim, 0xFF, h->claim_cells * sizeof(uint32_t), h->stream));
+    CK(cudaMemsetAsync(h->d_err, 0, sizeof(int), h->stream));
+    rc = push_params(h);
+    if (rc) return rc;
+    LAUNCH(kKBuildPlane, (k_build_plane<<<blocks_for(h->slots), kThreads, 0, h->stream>>>(
+                              h->d_params, h->d_chunk_rep, h->slots, h->d_pos, h->d_st, h->d_plane, h->d_err)));
+    CK(cudaStreamSynchronize(h->stream));  // the host mirrors go out of scope
+    rc = harvest_events(h);
+    if (rc) return rc;
+    return check_error_flag(h);
 }
 
-static int push_params(epi_engine* h) {
-    CK(cudaMemcpyAsync(h->d_params, &h->hp, sizeof(DevParams), cudaMemcpyHostToDevice, h->stream));
-    CK(cudaStreamSynchronize(h->stream));
+// World builds of R configurations on the host, in parallel.
+static int build_worlds(const epi_params* params, uint32_t R, std::vector<std::vector<epi_agent_record>>& worlds,
+                        std::string& err) {
+    worlds.assign(R, {});
+    std::vector<int> status(R, EPI_OK);
+    std::vector<std::string> errs(R);
+    const unsigned workers = std::max(1u, std::min<unsigned>(R, std::thread::hardware_concurrency()));
+    std::vector<std::thread> pool;
+    for (unsigned w = 0; w < workers; ++w)
+        pool.emplace_back([&, w] {
+            for (uint32_t r = w; r < R; r += workers) {
+                epi_geography g;
+                status[r] = build_world(params[r], worlds[r], g, errs[r]);
+            }
+        });
+    for (auto& t : pool) t.join();
+    for (uint32_t r = 0; r < R; ++r)
+        if (status[r]) {
+            err = (R > 1 ? "replicate " + std::to_string(r) + ": " : std::string()) + errs[r];
+            return status[r];
+        }
     return EPI_OK;
 }
 
-static int finish_bulk(epi_engine* h) {
+static int snapshot_replica(epi_engine* h, uint32_t r, epi_agent_record* out, size_t n) {
+    const Replica& rep = h->reps[r];
+    if (!out || n != rep.n) return EPI_ERR_ARG;
+    const size_t off = rep.hp.agent_off;
+    std::vector<uint32_t> pos(n), home(n), work(n), wsa(n);
+    std::vector<uint2> st(n);
+    CK(cudaMemcpyAsync(pos.data(), h->d_pos + off, n * sizeof(uint32_t), cudaMemcpyDeviceToHost, h->stream));
+    CK(cudaMemcpyAsync(home.data(), h->d_home + off, n * sizeof(uint32_t), cudaMemcpyDeviceToHost, h->stream));
+    CK(cudaMemcpyAsync(work.data(), h->d_work + off, n * sizeof(uint32_t), cudaMemcpyDeviceToHost, h->stream));
+    CK(cudaMemcpyAsync(wsa.data(), h->d_wsa + off, n * sizeof(uint32_t), cudaMemcpyDeviceToHost, h->stream));
+    CK(cudaMemcpyAsync(st.data(), h->d_st + off, n * sizeof(uint2), cudaMemcpyDeviceToHost, h->stream));
     CK(cudaStreamSynchronize(h->stream));
-    h->kernels_launched += 1;
-    return harvest_events(h);
+    for (size_t i = 0; i < n; ++i) {
+        epi_agent_record& a = out[i];
+        std::memset(&a, 0, sizeof a);
+        const uint32_t s = st[i].x, v = s & kStateMask;
+        a.x = unpack_x(pos[i]);
+        a.y = unpack_y(pos[i]);
+        a.state = (uint8_t)v;
+        a.flags = (uint8_t)(((s & kHosp) ? EPI_F_HOSPITALIZED : 0) | ((s & kIso) ? EPI_F_ISOLATED : 0) |
+                            ((s & kVacc) ? EPI_F_VACCINATED : 0) | ((s & kWq) ? EPI_F_WORK_QUARANTINED : 0) |
+                            ((s & kPt) ? EPI_F_PUBLIC_TRANSPORT : 0));
+        a.work_status = (uint8_t)st_ws(s);
+        a.immunity = (int8_t)st_imm(s);
+        a.at_hour = (v == EPI_E || v == EPI_I_PRE) ? st[i].y : 0u;
+        a.infection_day = infected(s) ? st_day(s) : 0u;
+        a.work_start_at = st_ws(s) == EPI_WS_HOSPITAL_STAFF ? wsa[i] : 0u;
+        a.home_x = unpack_x(home[i]);
+        a.home_y = unpack_y(home[i]);
+        a.work_x = unpack_x(work[i]);
+        a.work_y = unpack_y(work[i]);
+        const uint32_t code = st_area(s);
+        Rect ar = code == kHome ? Rect{a.home_x, a.home_y, a.home_x + 1, a.home_y + 1}
+                  : code == kWork ? Rect{a.work_x, a.work_y, a.work_x + 9, a.work_y + 9}
+                                  : rep.hp.area[code < kNumAreas ? code : kHome];
+        a.area_x0 = ar.x0; a.area_y0 = ar.y0; a.area_x1 = ar.x1; a.area_y1 = ar.y1;
+    }
+    return EPI_OK;
 }
 
-// ------------------------------------------------------------------ C ABI
+static int check_all(epi_engine* h) {
+    CK(cudaMemsetAsync(h->d_scratch, 0, 4 * sizeof(unsigned long long), h->stream));
+    LAUNCH(kKCheck, (k_check_agents<<<blocks_for(h->slots), kThreads, 0, h->stream>>>(
+                         h->d_params, h->d_chunk_rep, h->slots, h->d_pos, h->d_st, h->d_plane, h->d_scratch)));
+    LAUNCH(kKCheck, (k_check_plane<<<h->grid_blocks, kThreads, 0, h->stream>>>(h->plane_bytes, h->d_plane, h->claim_cells,
+                                                                                h->d_claim, h->d_scratch + 1,
+                                                                                h->d_scratch + 2)));
+    unsigned long long v[4] = {0, 0, 0, 0};
+    CK(cudaMemcpyAsync(v, h->d_scratch, sizeof v, cudaMemcpyDeviceToHost, h->stream));
+    CK(cudaStreamSynchronize(h->stream));
+    int rc = harvest_events(h);
+    if (rc) return rc;
+    uint64_t population = 0;
+    for (const auto& rep : h->reps) population += rep.n;
+    if (v[0] || v[1] != population || v[2]) {
+        h->err = "invariants: " + std::to_string(v[0]) + " agents off their cell class, " + std::to_string(v[1]) +
+                 " occupied cells for " + std::to_string(population) + " agents, " + std::to_string(v[2]) + " stale claims";
+        return EPI_ERR_INVARIANT;
+    }
+    return EPI_OK;
+}
+
+static int save_state(epi_engine* h) {
+    const size_t n = h->slots;
+    if (!h->s_pos) {
+        CK(cudaMalloc(&h->s_pos, n * sizeof(uint32_t)));
+        CK(cudaMalloc(&h->s_wsa, n * sizeof(uint32_t)));
+        CK(cudaMalloc(&h->s_st, n * sizeof(uint2)));
+        CK(cudaMalloc(&h->s_plane, h->plane_bytes));
+    }
+    CK(cudaMemcpyAsync(h->s_pos, h->d_pos, n * sizeof(uint32_t), cudaMemcpyDeviceToDevice, h->stream));
+    CK(cudaMemcpyAsync(h->s_wsa, h->d_wsa, n * sizeof(uint32_t), cudaMemcpyDeviceToDevice, h->stream));
+    CK(cudaMemcpyAsync(h->s_st, h->d_st, n * sizeof(uint2), cudaMemcpyDeviceToDevice, h->stream));
+    CK(cudaMemcpyAsync(h->s_plane, h->d_plane, h->plane_bytes, cudaMemcpyDeviceToDevice, h->stream));
+    CK(cudaStreamSynchronize(h->stream));
+    for (auto& rep : h->reps) {
+        rep.s_iv = rep.iv;
+        rep.s_geo = rep.geo;
+        rep.s_hosp_code = rep.hp.hosp_code;
+        rep.s_active = rep.active;
+    }
+    h->saved = true;
+    return EPI_OK;
+}
+
+static int restore_state(epi_engine* h) {
+    if (!h->saved) { h->err = "no saved state"; return EPI_ERR_ARG; }
+    const size_t n = h->slots;
+    CK(cudaMemcpyAsync(h->d_pos, h->s_pos, n * sizeof(uint32_t), cudaMemcpyDeviceToDevice, h->stream));
+    CK(cudaMemcpyAsync(h->d_wsa, h->s_wsa, n * sizeof(uint32_t), cudaMemcpyDeviceToDevice, h->stream));
+    CK(cudaMemcpyAsync(h->d_st, h->s_st, n * sizeof(uint2), cudaMemcpyDeviceToDevice, h->stream));
+    CK(cudaMemcpyAsync(h->d_plane, h->s_plane, h->plane_bytes, cudaMemcpyDeviceToDevice, h->stream));
+    CK(cudaMemsetAsync(h->d_tgt, 0xFF, n * sizeof(uint32_t), h->stream));
+    for (auto& rep : h->reps) {
+        rep.iv = rep.s_iv;
+        rep.geo = rep.s_geo;
+        rep.hp.hosp_code = rep.s_hosp_code;
+        rep.active = rep.s_active;
+        rep.hp.active = rep.s_active ? 1u : 0u;
+        rep.rows.clear();
+    }
+    return push_params(h);
+}
+
+static int create_engine(const epi_params* params, const epi_agent_record* const* recs, uint32_t R, epi_engine** out) {
+    epi_engine* h = new epi_engine();
+    int rc = engine_init(h, params, recs, R);
+    if (rc) {
+        g_create_error = h->err;
+        free_device(h);
+        delete h;
+        return rc;
+    }
+    *out = h;
+    return EPI_OK;
+}
+
+// ------------------------------------------------------------------ C ABI: config, geography, world
 extern "C" {
 
 int epi_params_from_json(const char* json_text, epi_params* out, char* err, size_t errlen) {
@@ -693,30 +806,26 @@ int epi_world_build(const epi_params* p, epi_agent_record* out, size_t n, epi_ge
     return EPI_OK;
 }
 
+// ------------------------------------------------------------------ C ABI: single engine
 int epi_engine_create_from_records(const epi_params* params, const epi_agent_record* recs, size_t n, epi_engine** out) {
     if (!params || !recs || !out) return EPI_ERR_ARG;
     *out = nullptr;
-    epi_engine* h = new epi_engine();
-    int rc = engine_init(h, *params, recs, n);
-    if (rc) {
-        g_create_error = h->err;
-        free_device(h);
-        delete h;
-        return rc;
+    if (n != params->number_of_agents || n == 0 || n >= 0xFFFFFFFFull) {
+        g_create_error = "record count != number_of_agents";
+        return EPI_ERR_ARG;
     }
-    *out = h;
-    return EPI_OK;
+    const epi_agent_record* one[1] = {recs};
+    return create_engine(params, one, 1, out);
 }
 
 int epi_engine_create(const epi_params* params, epi_engine** out) {
     if (!params || !out) return EPI_ERR_ARG;
     *out = nullptr;
-    std::vector<epi_agent_record> recs;
-    epi_geography g;
+    std::vector<std::vector<epi_agent_record>> worlds;
     std::string err;
-    int rc = build_world(*params, recs, g, err);
+    int rc = build_worlds(params, 1, worlds, err);
     if (rc) { g_create_error = err; return rc; }
-    return epi_engine_create_from_records(params, recs.data(), recs.size(), out);
+    return epi_engine_create_from_records(params, worlds[0].data(), worlds[0].size(), out);
 }
 
 int epi_engine_create_json(const char* config_json, uint64_t seed, epi_engine** out) {
@@ -752,86 +861,51 @@ int epi_engine_set_stream(epi_engine* h, void* cuda_stream) {
     return EPI_OK;
 }
 
-int epi_engine_simulate(epi_engine* h, uint32_t hour, epi_counts* out) {
-    if (!h || !out) return EPI_ERR_ARG;
-    return run_hours(h, hour, 1, out);
-}
-
 int epi_engine_simulate_hours(epi_engine* h, uint32_t first_hour, uint32_t n, epi_counts* out) {
     if (!h || (!out && n)) return EPI_ERR_ARG;
-    return run_hours(h, first_hour, n, out);
+    int rc = run_hours(h, first_hour, n);
+    if (rc) return rc;
+    for (uint32_t k = 0; k < n; ++k) out[k] = counts_of(h, k, 0, first_hour + k);
+    return EPI_OK;
 }
 
-int epi_engine_lock_city(epi_engine* h) {
-    if (!h) return EPI_ERR_ARG;
-    LAUNCH(kKLock, (k_lock<<<h->grid_blocks, kThreads, 0, h->stream>>>(h->d_params, h->d_st, 1)));
-    return finish_bulk(h);
+int epi_engine_simulate(epi_engine* h, uint32_t hour, epi_counts* out) {
+    if (!h || !out) return EPI_ERR_ARG;
+    return epi_engine_simulate_hours(h, hour, 1, out);
 }
 
-int epi_engine_unlock_city(epi_engine* h) {
-    if (!h) return EPI_ERR_ARG;
-    LAUNCH(kKLock, (k_lock<<<h->grid_blocks, kThreads, 0, h->stream>>>(h->d_params, h->d_st, 0)));
-    return finish_bulk(h);
-}
+int epi_engine_lock_city(epi_engine* h) { return h ? lock_city(h, 0, 1) : EPI_ERR_ARG; }
+int epi_engine_unlock_city(epi_engine* h) { return h ? lock_city(h, 0, 0) : EPI_ERR_ARG; }
 
 int epi_engine_vaccinate(epi_engine* h, uint32_t hour, double percent) {
     if (!h || !(percent >= 0.0 && percent <= 1.0)) return EPI_ERR_ARG;
-    const uint64_t thr = bernoulli_threshold(percent);
-    LAUNCH(kKVaccinate, (k_vaccinate<<<h->grid_blocks, kThreads, 0, h->stream>>>(h->d_params, h->d_st, hour, thr)));
-    return finish_bulk(h);
+    return vaccinate(h, 0, hour, percent);
 }
 
 int epi_engine_increase_hospital_size(epi_engine* h) {
     if (!h) return EPI_ERR_ARG;
-    const epi_area grown = grown_hospital(h->geo0);
-    h->geo.hospital = grown;
-    h->hp.hosp_code = rect_eq(to_rect(grown), h->hp.area[kHosp0]) ? kHosp0 : kHosp1;
+    grow_hospital(h, 0);
     return push_params(h);
 }
 
 int epi_engine_process_interventions(epi_engine* h, const epi_counts* counts, uint32_t* applied) {
     if (!h || !counts) return EPI_ERR_ARG;
-    InterventionActions a = decide_interventions(h->p, h->iv, *counts, h->geo.hospital);
-    int rc = EPI_OK;
-    if (a.vaccinate && (rc = epi_engine_vaccinate(h, counts->hour, a.vaccinate_percent))) return rc;
-    if (a.lock && (rc = epi_engine_lock_city(h))) return rc;
-    if (a.unlock && (rc = epi_engine_unlock_city(h))) return rc;
-    if (a.grow_hospital && (rc = epi_engine_increase_hospital_size(h))) return rc;
-    if (applied) *applied = a.applied;
-    return EPI_OK;
+    bool dirty = false;
+    int rc = process_interventions(h, 0, *counts, applied, &dirty);
+    if (rc) return rc;
+    return dirty ? push_params(h) : EPI_OK;
 }
 
 int epi_engine_run(epi_engine* h, epi_counts* rows, uint32_t max_rows, uint32_t* n_rows) {
     if (!h || !n_rows) return EPI_ERR_ARG;
     *n_rows = 0;
-    h->rows.clear();
-    const uint32_t hours = h->p.hours;
-    std::vector<epi_counts> seg;
-    uint32_t hour = 1;
-    bool stop = false;
-    while (hour < hours && !stop) {
-        uint32_t end = hour;  // last hour of the segment: next intervention point or the last hour
-        while (end + 1 < hours && !is_event_hour(h->p, end)) ++end;
-        const uint32_t nh = end - hour + 1;
-        seg.resize(nh);
-        int rc = run_hours(h, hour, nh, seg.data());
-        if (rc) return rc;
-        for (uint32_t k = 0; k < nh; ++k) {
-            h->rows.push_back(seg[k]);
-            // interventions can only fire at the segment's last hour (an event hour)
-            if (k + 1 == nh) {
-                rc = epi_engine_process_interventions(h, &seg[k], nullptr);
-                if (rc) return rc;
-            }
-            // stop_simulation, epidemiology_simulation.rs:564-575 (standalone)
-            if (seg[k].exposed == 0 && seg[k].infected == 0 && seg[k].hospitalized == 0) { stop = true; break; }
-        }
-        hour = end + 1;
-    }
-    const uint32_t nr = (uint32_t)h->rows.size();
+    int rc = run_loop(h);
+    if (rc) return rc;
+    const std::vector<epi_counts>& got = h->reps[0].rows;
+    const uint32_t nr = (uint32_t)got.size();
     if (rows) {
         if (max_rows < nr) { h->err = "rows buffer too small"; return EPI_ERR_ARG; }
-        std::memcpy(rows, h->rows.data(), nr * sizeof(epi_counts));
+        std::memcpy(rows, got.data(), nr * sizeof(epi_counts));
     }
     *n_rows = nr;
     return EPI_OK;
@@ -839,118 +913,29 @@ int epi_engine_run(epi_engine* h, epi_counts* rows, uint32_t max_rows, uint32_t*
 
 int epi_engine_write_outputs(epi_engine* h, const char* dir, const char* engine_id) {
     if (!h || !dir || !engine_id) return EPI_ERR_ARG;
-    return write_outputs(dir, engine_id, h->rows, h->iv.reports, h->err);
+    return write_outputs(dir, engine_id, h->reps[0].rows, h->reps[0].iv.reports, h->err);
 }
 
 int epi_engine_population(const epi_engine* h, uint32_t* out) {
     if (!h || !out) return EPI_ERR_ARG;
-    *out = h->n;
+    *out = h->reps[0].n;
     return EPI_OK;
 }
 
 int epi_engine_geography(const epi_engine* h, epi_geography* out) {
     if (!h || !out) return EPI_ERR_ARG;
-    *out = h->geo;
+    *out = h->reps[0].geo;
     return EPI_OK;
 }
 
 int epi_engine_snapshot(epi_engine* h, epi_agent_record* out, size_t n) {
-    if (!h || !out || n != h->n) return EPI_ERR_ARG;
-    std::vector<uint32_t> pos(n), home(n), work(n), wsa(n);
-    std::vector<uint2> st(n);
-    CK(cudaMemcpyAsync(pos.data(), h->d_pos, n * sizeof(uint32_t), cudaMemcpyDeviceToHost, h->stream));
-    CK(cudaMemcpyAsync(home.data(), h->d_home, n * sizeof(uint32_t), cudaMemcpyDeviceToHost, h->stream));
-    CK(cudaMemcpyAsync(work.data(), h->d_work, n * sizeof(uint32_t), cudaMemcpyDeviceToHost, h->stream));
-    CK(cudaMemcpyAsync(wsa.data(), h->d_wsa, n * sizeof(uint32_t), cudaMemcpyDeviceToHost, h->stream));
-    CK(cudaMemcpyAsync(st.data(), h->d_st, n * sizeof(uint2), cudaMemcpyDeviceToHost, h->stream));
-    CK(cudaStreamSynchronize(h->stream));
-    for (size_t i = 0; i < n; ++i) {
-        epi_agent_record& r = out[i];
-        std::memset(&r, 0, sizeof r);
-        const uint32_t s = st[i].x, v = s & kStateMask;
-        r.x = unpack_x(pos[i]);
-        r.y = unpack_y(pos[i]);
-        r.state = (uint8_t)v;
-        r.flags = (uint8_t)(((s & kHosp) ? EPI_F_HOSPITALIZED : 0) | ((s & kIso) ? EPI_F_ISOLATED : 0) |
-                            ((s & kVacc) ? EPI_F_VACCINATED : 0) | ((s & kWq) ? EPI_F_WORK_QUARANTINED : 0) |
-                            ((s & kPt) ? EPI_F_PUBLIC_TRANSPORT : 0));
-        r.work_status = (uint8_t)st_ws(s);
-        r.immunity = (int8_t)st_imm(s);
-        r.at_hour = (v == EPI_E || v == EPI_I_PRE) ? st[i].y : 0u;
-        r.infection_day = infected(s) ? st_day(s) : 0u;
-        r.work_start_at = st_ws(s) == EPI_WS_HOSPITAL_STAFF ? wsa[i] : 0u;
-        r.home_x = unpack_x(home[i]);
-        r.home_y = unpack_y(home[i]);
-        r.work_x = unpack_x(work[i]);
-        r.work_y = unpack_y(work[i]);
-        const uint32_t code = st_area(s);
-        Rect a = code == kHome ? Rect{r.home_x, r.home_y, r.home_x + 1, r.home_y + 1}
-                 : code == kWork ? Rect{r.work_x, r.work_y, r.work_x + 9, r.work_y + 9}
-                                 : h->hp.area[code < kNumAreas ? code : kHome];
-        r.area_x0 = a.x0; r.area_y0 = a.y0; r.area_x1 = a.x1; r.area_y1 = a.y1;
-    }
-    return EPI_OK;
+    if (!h) return EPI_ERR_ARG;
+    return snapshot_replica(h, 0, out, n);
 }
 
-int epi_engine_check(epi_engine* h) {
-    if (!h) return EPI_ERR_ARG;
-    CK(cudaMemsetAsync(h->d_scratch, 0, 4 * sizeof(unsigned long long), h->stream));
-    LAUNCH(kKCheck, (k_check_agents<<<h->grid_blocks, kThreads, 0, h->stream>>>(h->d_params, h->d_pos, h->d_st, h->d_plane,
-                                                                                 h->d_scratch)));
-    LAUNCH(kKCheck, (k_check_plane<<<h->grid_blocks, kThreads, 0, h->stream>>>(h->plane_bytes, h->d_plane, h->claim_cells, h->d_claim,
-                                                                                h->d_scratch + 1, h->d_scratch + 2)));
-    unsigned long long v[4] = {0, 0, 0, 0};
-    CK(cudaMemcpyAsync(v, h->d_scratch, sizeof v, cudaMemcpyDeviceToHost, h->stream));
-    CK(cudaStreamSynchronize(h->stream));
-    int rc = harvest_events(h);
-    if (rc) return rc;
-    if (v[0] || v[1] != h->n || v[2]) {
-        h->err = "invariants: " + std::to_string(v[0]) + " agents off their cell class, " + std::to_string(v[1]) +
-                 " occupied cells for " + std::to_string(h->n) + " agents, " + std::to_string(v[2]) + " stale claims";
-        return EPI_ERR_INVARIANT;
-    }
-    return EPI_OK;
-}
-
-int epi_engine_save_state(epi_engine* h) {
-    if (!h) return EPI_ERR_ARG;
-    const size_t n = h->n;
-    if (!h->s_pos) {
-        CK(cudaMalloc(&h->s_pos, n * sizeof(uint32_t)));
-        CK(cudaMalloc(&h->s_wsa, n * sizeof(uint32_t)));
-        CK(cudaMalloc(&h->s_st, n * sizeof(uint2)));
-        CK(cudaMalloc(&h->s_plane, h->plane_bytes));
-    }
-    CK(cudaMemcpyAsync(h->s_pos, h->d_pos, n * sizeof(uint32_t), cudaMemcpyDeviceToDevice, h->stream));
-    CK(cudaMemcpyAsync(h->s_wsa, h->d_wsa, n * sizeof(uint32_t), cudaMemcpyDeviceToDevice, h->stream));
-    CK(cudaMemcpyAsync(h->s_st, h->d_st, n * sizeof(uint2), cudaMemcpyDeviceToDevice, h->stream));
-    CK(cudaMemcpyAsync(h->s_plane, h->d_plane, h->plane_bytes, cudaMemcpyDeviceToDevice, h->stream));
-    CK(cudaStreamSynchronize(h->stream));
-    h->s_iv = h->iv;
-    h->s_hosp_code = h->hp.hosp_code;
-    h->s_geo = h->geo;
-    h->saved = true;
-    return EPI_OK;
-}
-
-int epi_engine_restore_state(epi_engine* h) {
-    if (!h) return EPI_ERR_ARG;
-    if (!h->saved) { h->err = "no saved state"; return EPI_ERR_ARG; }
-    const size_t n = h->n;
-    CK(cudaMemcpyAsync(h->d_pos, h->s_pos, n * sizeof(uint32_t), cudaMemcpyDeviceToDevice, h->stream));
-    CK(cudaMemcpyAsync(h->d_wsa, h->s_wsa, n * sizeof(uint32_t), cudaMemcpyDeviceToDevice, h->stream));
-    CK(cudaMemcpyAsync(h->d_st, h->s_st, n * sizeof(uint2), cudaMemcpyDeviceToDevice, h->stream));
-    CK(cudaMemcpyAsync(h->d_plane, h->s_plane, h->plane_bytes, cudaMemcpyDeviceToDevice, h->stream));
-    h->iv = h->s_iv;
-    h->geo = h->s_geo;
-    if (h->hp.hosp_code != h->s_hosp_code) {
-        h->hp.hosp_code = h->s_hosp_code;
-        CK(cudaMemcpyAsync(h->d_params, &h->hp, sizeof(DevParams), cudaMemcpyHostToDevice, h->stream));
-    }
-    CK(cudaStreamSynchronize(h->stream));
-    h->rows.clear();
-    return EPI_OK;
-}
+int epi_engine_check(epi_engine* h) { return h ? check_all(h) : EPI_ERR_ARG; }
+int epi_engine_save_state(epi_engine* h) { return h ? save_state(h) : EPI_ERR_ARG; }
+int epi_engine_restore_state(epi_engine* h) { return h ? restore_state(h) : EPI_ERR_ARG; }
 
 int epi_engine_kernels_launched(const epi_engine* h, uint64_t* out) {
     if (!h || !out) return EPI_ERR_ARG;
@@ -983,18 +968,100 @@ size_t epi_abi_struct_size(const char* name) {
     return 0;
 }
 
-// Algorithmic bytes of one hour (the roofline numerator): the agent words the hour's
-// kernels must read and write plus one pass over the occupancy plane.
-//   movement hours and hours 0/23:  decide reads pos 4 + st 8 + home 4 + work 4, writes
-//   st 8 + tgt 4; commit reads tgt 4 + pos 4, writes pos 4; plane (G+1)^2 bytes read once.
+// Algorithmic bytes of one hour over all replicates (the roofline numerator): the agent
+// words the hour's kernels must read and write plus one pass over each occupancy plane.
+//   movement hours and hours 0/23: decide reads pos 4 + st 8 + home 4 + work 4, writes st 8 +
+//   tgt 4; commit reads tgt 4 + pos 4, writes pos 4; plane (G+1)^2 bytes read once.
 //   sleep hours: st.x read 4 (+ write 4 on the first sleep hour).
 int epi_engine_hour_bytes(const epi_engine* h, uint32_t hour, double* bytes) {
     if (!h || !bytes) return EPI_ERR_ARG;
     const uint32_t hod = hour % 24u;
-    const double n = (double)h->n;
-    if (hod >= 1u && hod <= 6u) *bytes = n * (hod == 1u ? 8.0 : 4.0);
-    else *bytes = n * 44.0 + (double)h->claim_cells;
+    double b = 0.0;
+    for (const auto& rep : h->reps) {
+        const double n = (double)rep.n, side = (double)rep.p.grid_size + 1.0;
+        if (hod >= 1u && hod <= 6u) b += n * (hod == 1u ? 8.0 : 4.0);
+        else b += n * 44.0 + side * side;
+    }
+    *bytes = b;
     return EPI_OK;
+}
+
+// ------------------------------------------------------------------ C ABI: ensemble
+int epi_ensemble_create(const epi_params* params, uint32_t replicates, epi_ensemble** out) {
+    if (!params || !out || replicates == 0) return EPI_ERR_ARG;
+    *out = nullptr;
+    std::vector<std::vector<epi_agent_record>> worlds;
+    std::string err;
+    int rc = build_worlds(params, replicates, worlds, err);
+    if (rc) { g_create_error = err; return rc; }
+    std::vector<const epi_agent_record*> recs(replicates);
+    for (uint32_t r = 0; r < replicates; ++r) recs[r] = worlds[r].data();
+    epi_ensemble* e = new epi_ensemble();
+    rc = engine_init(&e->core, params, recs.data(), replicates);
+    if (rc) {
+        g_create_error = e->core.err;
+        free_device(&e->core);
+        delete e;
+        return rc;
+    }
+    *out = e;
+    return EPI_OK;
+}
+
+void epi_ensemble_destroy(epi_ensemble* e) {
+    if (!e) return;
+    free_device(&e->core);
+    delete e;
+}
+
+const char* epi_ensemble_last_error(const epi_ensemble* e) { return e ? e->core.err.c_str() : g_create_error.c_str(); }
+
+int epi_ensemble_set_stream(epi_ensemble* e, void* cuda_stream) {
+    return e ? epi_engine_set_stream(&e->core, cuda_stream) : EPI_ERR_ARG;
+}
+
+int epi_ensemble_run(epi_ensemble* e, epi_counts* rows, uint32_t max_rows_per_replicate, uint32_t* n_rows) {
+    if (!e || !n_rows) return EPI_ERR_ARG;
+    epi_engine* h = &e->core;
+    int rc = run_loop(h);
+    if (rc) return rc;
+    for (uint32_t r = 0; r < h->R(); ++r) {
+        const std::vector<epi_counts>& got = h->reps[r].rows;
+        n_rows[r] = (uint32_t)got.size();
+        if (rows) {
+            if (got.size() > max_rows_per_replicate) { h->err = "rows buffer too small"; return EPI_ERR_ARG; }
+            std::memcpy(rows + (size_t)r * max_rows_per_replicate, got.data(), got.size() * sizeof(epi_counts));
+        }
+    }
+    return EPI_OK;
+}
+
+int epi_ensemble_replicates(const epi_ensemble* e, uint32_t* out) {
+    if (!e || !out) return EPI_ERR_ARG;
+    *out = e->core.R();
+    return EPI_OK;
+}
+
+int epi_ensemble_snapshot(epi_ensemble* e, uint32_t replicate, epi_agent_record* out, size_t n) {
+    if (!e || replicate >= e->core.R()) return EPI_ERR_ARG;
+    return snapshot_replica(&e->core, replicate, out, n);
+}
+
+int epi_ensemble_check(epi_ensemble* e) { return e ? check_all(&e->core) : EPI_ERR_ARG; }
+int epi_ensemble_save_state(epi_ensemble* e) { return e ? save_state(&e->core) : EPI_ERR_ARG; }
+int epi_ensemble_restore_state(epi_ensemble* e) { return e ? restore_state(&e->core) : EPI_ERR_ARG; }
+int epi_ensemble_set_profiling(epi_ensemble* e, int on) { return e ? epi_engine_set_profiling(&e->core, on) : EPI_ERR_ARG; }
+
+int epi_ensemble_kernel_stats(const epi_ensemble* e, uint32_t* launches, double* total_ms, int n) {
+    return e ? epi_engine_kernel_stats(&e->core, launches, total_ms, n) : EPI_ERR_ARG;
+}
+
+int epi_ensemble_kernels_launched(const epi_ensemble* e, uint64_t* out) {
+    return e ? epi_engine_kernels_launched(&e->core, out) : EPI_ERR_ARG;
+}
+
+int epi_ensemble_hour_bytes(const epi_ensemble* e, uint32_t hour, double* bytes) {
+    return e ? epi_engine_hour_bytes(&e->core, hour, bytes) : EPI_ERR_ARG;
 }
 
 }  // extern "C"
@@ -1030,32 +1097,8 @@ size_t align256(size_t v) { return (v + 255) & ~size_t(255); }
 DevParams noalloc_params(const epi_params& p, uint32_t hospital_grown) {
     epi_geography g = define_geography(p.grid_size);
     resize_hospital(g, (int32_t)p.number_of_agents, 0.002, p.hospital_beds_percentage);
-    DevParams d;
-    std::memset(&d, 0, sizeof d);
-    d.n = p.number_of_agents;
-    d.G = (int32_t)p.grid_size;
-    d.W = d.G + 1;
-    d.WP = d.G + 3;
-    d.area[kTransport] = to_rect(g.transport);
-    d.area[kHousing] = to_rect(g.housing);
-    d.area[kHosp0] = to_rect(g.hospital);
-    d.area[kHosp1] = to_rect(grown_hospital(g));
+    DevParams d = make_dev_params(p, g, p.number_of_agents);
     d.hosp_code = (hospital_grown && !rect_eq(d.area[kHosp1], d.area[kHosp0])) ? kHosp1 : kHosp0;
-    d.key0 = (uint32_t)p.seed;
-    d.key1 = (uint32_t)(p.seed >> 32);
-    d.reg_start = p.regular_transmission_start_day;
-    d.high_start = p.high_transmission_start_day;
-    d.last_day = p.last_day;
-    d.exposed_duration = p.exposed_duration;
-    d.pre_duration = p.pre_symptomatic_duration;
-    const double rates[3] = {0.0, p.regular_transmission_rate, p.high_transmission_rate};
-    for (int c = 0; c < 3; ++c) {
-        d.thr_rate[c] = bernoulli_threshold(rates[c]);
-        if (rates[c] >= p.high_transmission_rate) d.hosp_if_class |= 1u << c;
-    }
-    d.thr_death = bernoulli_threshold(p.death_rate);
-    d.thr_symptoms = bernoulli_threshold(1.0 - p.percentage_asymptomatic_population);
-    d.thr_severe = bernoulli_threshold(p.percentage_severe_infected_population);
     return d;
 }
 
@@ -1127,15 +1170,16 @@ extern "C" int epi_tick_hour_noalloc(const epi_params* params, uint32_t hour, ui
     NOALLOC_CK(cudaMemsetAsync(d_err, 0, sizeof(int), s));
     NOALLOC_CK(cudaMemsetAsync(counts, 0, 8 * sizeof(uint32_t), s));
     uint2* st = reinterpret_cast<uint2*>(state);
-    const int blocks = (int)std::min<uint64_t>(((uint64_t)n + kThreads - 1) / kThreads, (uint64_t)d->grid_blocks);
+    const uint32_t n_chunks = (n + kChunk - 1) / kChunk;
+    const int blocks = (int)std::min<uint64_t>(n_chunks, (uint64_t)d->grid_blocks);
     const uint32_t hod = hour % 24u;
     if (hod >= 1u && hod <= 6u) {
-        k_sleep<<<blocks, kThreads, 0, s>>>(d_params, st, counts);
+        k_sleep<<<blocks, kThreads, 0, s>>>(d_params, nullptr, n_chunks, st, counts);
     } else {
         NOALLOC_CK(cudaMemsetAsync(d_claim, 0xFF, claim_bytes, s));
-        k_decide<<<blocks, kThreads, 0, s>>>(d_params, pos, st, home, work, work_start_at, plane, d_claim, d_tgt, counts,
-                                             d_hour, 0u, d_err);
-        k_commit<<<(int)(((uint64_t)n + kThreads - 1) / kThreads), kThreads, 0, s>>>(d_params, pos, d_tgt, plane, d_claim);
+        k_decide<<<blocks, kThreads, 0, s>>>(d_params, nullptr, n_chunks, pos, st, home, work, work_start_at, plane, d_claim,
+                                             d_tgt, counts, d_hour, 0u, d_err);
+        k_commit<<<(int)n_chunks, kThreads, 0, s>>>(d_params, nullptr, n, pos, d_tgt, plane, d_claim);
     }
     NOALLOC_CK(cudaGetLastError());
     int err = 0;

@@ -84,7 +84,14 @@ struct DevParams {
     uint32_t hosp_if_class;     // bit c: rate of class c >= high rate (c = 0 none, 1 reg, 2 high)
     uint64_t thr_rate[3];       // Bernoulli thresholds of the rate classes
     uint64_t thr_death, thr_symptoms, thr_severe;
+    // placement of this world among the replicates sharing the device arrays
+    uint32_t agent_off;         // first agent slot (a multiple of the 256-slot chunk)
+    uint32_t active;            // 0 once the run of this replicate has ended
+    uint64_t plane_off;         // byte offset of its bordered plane
+    uint64_t claim_off;         // word offset of its claim plane
 };
+
+constexpr uint32_t kChunk = 256;  // agent slots per chunk; replicates start on chunk boundaries
 
 // Bernoulli(p) as a threshold on a uniform 32-bit word: gen_bool(p) <=> u < thr.
 inline uint64_t bernoulli_threshold(double p) {

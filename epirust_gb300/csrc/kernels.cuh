@@ -1,0 +1,284 @@
+// kernels.cuh -- the sm_103a kernels of the hourly tick, over one or many replicates.
+//
+// Agent slots of all replicates are concatenated; each replicate starts on a 256-slot chunk
+// boundary, so a chunk belongs to one replicate (chunk_rep[c]; absent when there is one).
+// The counting kernels walk chunks with a grid-stride loop, stage the chunk's replicate
+// parameters in shared memory and flush their per-block histogram whenever the replicate
+// changes; the commit kernel runs one thread per slot.  Philox counters and claim values use
+// the agent's index within its replicate, so a replicate evolves exactly as a lone engine
+// with the same parameters would.
+//
+// Per simulated hour (CitizenLocationMap::simulate, engine/src/allocation_map.rs:67-129):
+//   hours 1..6 of a day   k_sleep   current_area = home (non-staff), counts
+//   other hours           k_decide  per-agent rules on the previous-hour plane, proposals,
+//                                   atomicMin claims on the target cells, counts
+//                         k_commit  lowest claimant moves, losers stay, plane bytes updated,
+//                                   claims released
+#pragma once
+
+#include "tick.cuh"
+
+namespace epi {
+namespace kern {
+
+constexpr int kThreads = (int)kChunk;
+
+// Warp-aggregated 6-bin histogram into shared memory.
+__device__ __forceinline__ void count_into(uint32_t* sh, bool valid, uint32_t bin) {
+    const int lane = threadIdx.x & 31;
+#pragma unroll
+    for (uint32_t b = 0; b < 6; ++b) {
+        uint32_t c = __popc(__ballot_sync(0xFFFFFFFFu, valid && bin == b));
+        if (lane == 0 && c) atomicAdd(&sh[b], c);
+    }
+}
+
+// Block-uniform bookkeeping of the replicate a block is working on.
+struct BlockRep {
+    uint32_t r = 0xFFFFFFFFu;
+};
+
+// Switch the block to replicate r: flush the histogram of the previous one into its counts
+// row (counts[r * 8 + bin]), stage r's parameters, clear the histogram.  Block-uniform.
+__device__ __forceinline__ void switch_rep(BlockRep& br, uint32_t r, const DevParams* __restrict__ Pall, DevParams& sP,
+                                           uint32_t* sh, uint32_t* counts) {
+    __syncthreads();
+    if (br.r != 0xFFFFFFFFu && threadIdx.x < 6 && sh[threadIdx.x]) atomicAdd(&counts[br.r * 8 + threadIdx.x], sh[threadIdx.x]);
+    __syncthreads();
+    for (uint32_t k = threadIdx.x; k < sizeof(DevParams) / 4; k += blockDim.x)
+        reinterpret_cast<uint32_t*>(&sP)[k] = reinterpret_cast<const uint32_t*>(Pall + r)[k];
+    if (threadIdx.x < 8) sh[threadIdx.x] = 0;
+    __syncthreads();
+    br.r = r;
+}
+
+__device__ __forceinline__ void flush_rep(const BlockRep& br, uint32_t* sh, uint32_t* counts) {
+    __syncthreads();
+    if (br.r != 0xFFFFFFFFu && threadIdx.x < 6 && sh[threadIdx.x]) atomicAdd(&counts[br.r * 8 + threadIdx.x], sh[threadIdx.x]);
+}
+
+// First vacant hospital cell of the snapshot in AreaIterator order (area.rs:221-237), found
+// by the whole block; kNoAction when the hospital is full.
+__device__ uint32_t block_first_vacant(const DevParams& P, const PlaneView& pl) {
+    __shared__ uint32_t best;
+    const Rect h = P.area[P.hosp_code];
+    const uint32_t w = (uint32_t)(h.x1 - h.x0 + 1), total = w * (uint32_t)(h.y1 - h.y0 + 1);
+    if (threadIdx.x == 0) best = kNoAction;
+    __syncthreads();
+    for (uint32_t base = 0; base < total; base += blockDim.x) {
+        const uint32_t c = base + threadIdx.x;
+        bool vac = false;
+        if (c < total) vac = pl.vacant(h.x0 + (int32_t)(c % w), h.y0 + (int32_t)(c / w));
+        if (vac) atomicMin(&best, c);
+        if (__syncthreads_or(vac)) break;
+    }
+    const uint32_t c = best;
+    __syncthreads();
+    if (c == kNoAction) return kNoAction;
+    return pack_xy(h.x0 + (int32_t)(c % w), h.y0 + (int32_t)(c / w));
+}
+
+// Hours 1..6 (SLEEP_START_TIME..=SLEEP_END_TIME, citizen/mod.rs:244-248).
+__global__ void __launch_bounds__(kThreads) k_sleep(const DevParams* __restrict__ Pall, const uint32_t* __restrict__ chunk_rep,
+                                                    uint32_t n_chunks, uint2* __restrict__ st, uint32_t* __restrict__ counts) {
+    __shared__ uint32_t sh[8];
+    __shared__ DevParams sP;
+    BlockRep br;
+    for (uint32_t c = blockIdx.x; c < n_chunks; c += gridDim.x) {
+        const uint32_t r = chunk_rep ? chunk_rep[c] : 0u;
+        if (r != br.r) switch_rep(br, r, Pall, sP, sh, counts);
+        if (!sP.active) continue;
+        const uint32_t slot = c * kChunk + threadIdx.x;
+        const bool valid = slot - sP.agent_off < sP.n;
+        uint32_t s = 0;
+        if (valid) {
+            s = st[slot].x;
+            if (st_ws(s) != EPI_WS_HOSPITAL_STAFF && st_area(s) != kHome) {
+                s = with_area(s, kHome);
+                st[slot].x = s;
+            }
+        }
+        count_into(sh, valid, count_bin(s));
+    }
+    flush_rep(br, sh, counts);
+}
+
+// One hour of per-agent rules (hour of day 0, 7..22 or 23).
+__global__ void __launch_bounds__(kThreads) k_decide(const DevParams* __restrict__ Pall, const uint32_t* __restrict__ chunk_rep,
+                                                     uint32_t n_chunks, const uint32_t* __restrict__ pos,
+                                                     uint2* __restrict__ st, const uint32_t* __restrict__ home,
+                                                     const uint32_t* __restrict__ work, uint32_t* __restrict__ wsa,
+                                                     const uint8_t* __restrict__ plane, uint32_t* __restrict__ claim,
+                                                     uint32_t* __restrict__ tgt, uint32_t* __restrict__ counts,
+                                                     const uint32_t* __restrict__ hour_base, uint32_t hour_offset,
+                                                     int* err) {
+    __shared__ uint32_t sh[8];
+    __shared__ DevParams sP;
+    const DevParams& P = sP;
+    const uint32_t hour = *hour_base + hour_offset;
+    const uint32_t hod = hour % 24u;
+    BlockRep br;
+    uint32_t hosp_first = kNoAction;
+    bool hosp_known = false;
+    for (uint32_t c = blockIdx.x; c < n_chunks; c += gridDim.x) {
+        const uint32_t r = chunk_rep ? chunk_rep[c] : 0u;
+        if (r != br.r) {
+            switch_rep(br, r, Pall, sP, sh, counts);
+            hosp_known = false;
+        }
+        if (!P.active) continue;
+        const PlaneView pl{plane + P.plane_off, P.G, P.WP, err};
+        uint32_t* rclaim = claim + P.claim_off;
+        const uint32_t slot = c * kChunk + threadIdx.x;
+        const uint32_t i = slot - P.agent_off;  // index within the replicate
+        const bool valid = i < P.n;
+        uint32_t s = 0, at = 0, p = 0;
+        if (valid) {
+            const uint2 sv = st[slot];
+            s = sv.x;
+            at = sv.y;
+            p = pos[slot];
+        }
+        if (hod == 0u) {
+            const bool need = valid && wants_hospital(P, infected(s) ? with_day(s, st_day(s) + 1u) : s);
+            if (__syncthreads_or(need) && !hosp_known) {
+                hosp_first = block_first_vacant(P, pl);
+                hosp_known = true;
+            }
+        }
+        uint32_t bin = 0;
+        if (valid) {
+            const uint32_t s0 = s, at0 = at;
+            const uint32_t hm = home[slot], wk = work[slot];
+            const Cell cell{unpack_x(p), unpack_y(p)};
+            Draws dr{i, hour, P.key0, P.key1};
+            Cell nc;
+            if (hod == 0u) {
+                nc = routine_start(P, pl, s, hm, cell, hosp_first, dr);
+            } else if (hod == 23u) {
+                nc = routine_end(P, pl, s, hm, cell, dr);
+            } else {
+                const bool staff = st_ws(s) == EPI_WS_HOSPITAL_STAFF;
+                uint32_t w0 = staff ? wsa[slot] : 0u, w = w0;
+                nc = perform_movements(P, pl, s, at, w, hm, wk, cell, hod, hour, dr);
+                if (staff && w != w0) wsa[slot] = w;
+            }
+            bool moving = nc.x != cell.x || nc.y != cell.y;
+            if (moving && ((uint32_t)nc.x > (uint32_t)P.G || (uint32_t)nc.y > (uint32_t)P.G)) {
+                atomicOr(err, 4);  // unreachable for validated worlds; never write outside the plane
+                moving = false;
+                nc = cell;
+            }
+            const uint32_t cls = cell_class(P, s);
+            if (moving) atomicMin(&rclaim[(size_t)nc.y * P.W + nc.x], i);
+            tgt[slot] = (moving || cls != cell_class(P, s0)) ? encode_target(nc, cls) : kNoAction;
+            if (s != s0 || at != at0) st[slot] = make_uint2(s, at);
+            bin = count_bin(s);
+        }
+        count_into(sh, valid, bin);
+    }
+    flush_rep(br, sh, counts);
+}
+
+// Resolve the claims of the hour: the lowest index that claimed a cell moves there
+// (the serial resolve of allocation_map.rs:93-102 in index order), others keep their cell.
+__global__ void __launch_bounds__(kThreads) k_commit(const DevParams* __restrict__ Pall, const uint32_t* __restrict__ chunk_rep,
+                                                     uint32_t n_slots, uint32_t* __restrict__ pos,
+                                                     const uint32_t* __restrict__ tgt, uint8_t* __restrict__ plane,
+                                                     uint32_t* __restrict__ claim) {
+    const uint32_t stride = gridDim.x * blockDim.x;
+    for (uint32_t slot = blockIdx.x * blockDim.x + threadIdx.x; slot < n_slots; slot += stride) {
+        const uint32_t t = tgt[slot];
+        if (t == kNoAction) continue;
+        const DevParams* Pr = Pall + (chunk_rep ? chunk_rep[slot / kChunk] : 0u);
+        if (!Pr->active) continue;
+        const uint32_t W = (uint32_t)Pr->W, WP = (uint32_t)Pr->WP;
+        uint8_t* rplane = plane + Pr->plane_off;
+        uint32_t* rclaim = claim + Pr->claim_off;
+        const uint32_t i = slot - Pr->agent_off;
+        const uint32_t p = pos[slot];
+        const uint32_t xy = target_xy(t), cls = target_class(t);
+        const size_t old_cell = (size_t)(unpack_y(p) + 1) * WP + (unpack_x(p) + 1);
+        if (xy != p) {
+            const size_t claim_cell = (size_t)unpack_y(xy) * W + unpack_x(xy);
+            if (rclaim[claim_cell] == i) {
+                rclaim[claim_cell] = kNoClaim;
+                rplane[old_cell] = 0;
+                rplane[(size_t)(unpack_y(xy) + 1) * WP + (unpack_x(xy) + 1)] = (uint8_t)cls;
+                pos[slot] = xy;
+                continue;
+            }
+        }
+        rplane[old_cell] = (uint8_t)cls;
+    }
+}
+
+// Plane bytes of every agent of every replicate (world upload).
+__global__ void k_build_plane(const DevParams* __restrict__ Pall, const uint32_t* __restrict__ chunk_rep, uint32_t n_slots,
+                              const uint32_t* __restrict__ pos, const uint2* __restrict__ st, uint8_t* __restrict__ plane,
+                              int* err) {
+    for (uint32_t slot = blockIdx.x * blockDim.x + threadIdx.x; slot < n_slots; slot += gridDim.x * blockDim.x) {
+        const DevParams& P = Pall[chunk_rep ? chunk_rep[slot / kChunk] : 0u];
+        if (slot - P.agent_off >= P.n) continue;
+        const uint32_t p = pos[slot];
+        const int32_t x = unpack_x(p), y = unpack_y(p);
+        if (x > P.G || y > P.G) { atomicOr(err, 2); continue; }
+        plane[P.plane_off + (size_t)(y + 1) * P.WP + (x + 1)] = (uint8_t)cell_class(P, st[slot].x);
+    }
+}
+
+// LockdownIntervention apply / revoke (allocation_map.rs:349-365) on slots [off, off + n).
+__global__ void k_lock(uint2* __restrict__ st, uint32_t off, uint32_t n, int on) {
+    for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
+        uint32_t s = st[off + i].x;
+        uint32_t ns = on ? (st_ws(s) != EPI_WS_ESSENTIAL ? (s | kIso) : s) : (s & ~kIso);
+        if (ns != s) st[off + i].x = ns;
+    }
+}
+
+// vaccinate (allocation_map.rs:381-387): susceptible agents with Philox block 3 word 0 < thr.
+__global__ void k_vaccinate(uint2* __restrict__ st, uint32_t off, uint32_t n, uint32_t key0, uint32_t key1,
+                            uint32_t hour, uint64_t thr) {
+    for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
+        uint32_t s = st[off + i].x;
+        if ((s & kStateMask) != EPI_S) continue;
+        uint32_t u[4];
+        philox4x32(i, hour, kBlkVaccine, 0u, key0, key1, u);
+        if ((uint64_t)u[0] < thr) st[off + i].x = s | kVacc;
+    }
+}
+
+// Invariants: each agent's cell holds its class.
+__global__ void k_check_agents(const DevParams* __restrict__ Pall, const uint32_t* __restrict__ chunk_rep,
+                               uint32_t n_slots, const uint32_t* __restrict__ pos, const uint2* __restrict__ st,
+                               const uint8_t* __restrict__ plane, unsigned long long* bad) {
+    for (uint32_t slot = blockIdx.x * blockDim.x + threadIdx.x; slot < n_slots; slot += gridDim.x * blockDim.x) {
+        const DevParams& P = Pall[chunk_rep ? chunk_rep[slot / kChunk] : 0u];
+        if (slot - P.agent_off >= P.n) continue;
+        const uint32_t p = pos[slot];
+        const int32_t x = unpack_x(p), y = unpack_y(p);
+        if (x > P.G || y > P.G || plane[P.plane_off + (size_t)(y + 1) * P.WP + (x + 1)] != cell_class(P, st[slot].x))
+            atomicAdd(bad, 1ull);
+    }
+}
+
+// Occupied plane bytes and taken claims over the whole buffers.
+__global__ void k_check_plane(size_t plane_bytes, const uint8_t* __restrict__ plane, size_t claim_cells,
+                              const uint32_t* __restrict__ claim, unsigned long long* occupied,
+                              unsigned long long* claimed) {
+    unsigned long long o = 0, c = 0;
+    const size_t stride = (size_t)gridDim.x * blockDim.x;
+    for (size_t k = blockIdx.x * (size_t)blockDim.x + threadIdx.x; k < plane_bytes; k += stride) o += plane[k] != 0;
+    for (size_t k = blockIdx.x * (size_t)blockDim.x + threadIdx.x; k < claim_cells; k += stride) c += claim[k] != kNoClaim;
+    for (int off = 16; off; off >>= 1) {
+        o += __shfl_down_sync(0xFFFFFFFFu, o, off);
+        c += __shfl_down_sync(0xFFFFFFFFu, c, off);
+    }
+    if ((threadIdx.x & 31) == 0) {
+        if (o) atomicAdd(occupied, o);
+        if (c) atomicAdd(claimed, c);
+    }
+}
+
+}  // namespace kern
+}  // namespace epi

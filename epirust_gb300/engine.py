@@ -92,9 +92,9 @@ def world_build(params: EpiParams) -> tuple[np.ndarray, EpiGeography]:
 class Epidemiology:
     """One single-region engine on the GPU."""
 
-    def __init__(self, config: Config, seed: int | None = None, records: np.ndarray | None = None):
-        self.config = config
-        self.params = EpiParams.from_buffer_copy(config.params)
+    def __init__(self, config: "Config | EpiParams", seed: int | None = None, records: np.ndarray | None = None):
+        self.config = config if isinstance(config, Config) else None
+        self.params = EpiParams.from_buffer_copy(config.params if isinstance(config, Config) else config)
         if seed is not None:
             self.params.seed = seed
         h = C.c_void_p()
@@ -220,4 +220,79 @@ class Epidemiology:
     def hour_bytes(self, hour: int) -> float:
         b = C.c_double(0.0)
         check(lib().epi_engine_hour_bytes(self._h, hour, C.byref(b)), self._h)
+        return b.value
+
+
+class Ensemble:
+    """Many independent worlds on one device, advanced together (epi_ensemble_*)."""
+
+    def __init__(self, params: list):
+        L = lib()
+        self.params = (EpiParams * len(params))(*[EpiParams.from_buffer_copy(p) for p in params])
+        h = C.c_void_p()
+        rc = L.epi_ensemble_create(self.params, len(params), C.byref(h))
+        if rc != _lib.EPI_OK:
+            raise _lib.EpiError(rc, L.epi_ensemble_last_error(None).decode())
+        self._h = h
+        self.replicates = len(params)
+
+    def _check(self, rc):
+        if rc != _lib.EPI_OK:
+            raise _lib.EpiError(rc, lib().epi_ensemble_last_error(self._h).decode())
+
+    def close(self) -> None:
+        if getattr(self, "_h", None):
+            lib().epi_ensemble_destroy(self._h)
+            self._h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def run(self) -> list:
+        """Per replicate: the structured counts rows of run_single_engine."""
+        cap = max(p.hours for p in self.params)
+        rows = np.zeros((self.replicates, max(cap, 1)), dtype=COUNTS_DTYPE)
+        n = np.zeros(self.replicates, dtype=np.uint32)
+        self._check(lib().epi_ensemble_run(self._h, rows.ctypes.data, rows.shape[1], n.ctypes.data))
+        return [rows[r, : n[r]] for r in range(self.replicates)]
+
+    def snapshot(self, r: int) -> np.ndarray:
+        out = np.zeros(self.params[r].number_of_agents, dtype=AGENT_DTYPE)
+        self._check(lib().epi_ensemble_snapshot(self._h, r, out.ctypes.data, len(out)))
+        return out
+
+    def check_invariants(self) -> None:
+        self._check(lib().epi_ensemble_check(self._h))
+
+    def save_state(self) -> None:
+        self._check(lib().epi_ensemble_save_state(self._h))
+
+    def restore_state(self) -> None:
+        self._check(lib().epi_ensemble_restore_state(self._h))
+
+    def set_stream(self, stream_ptr: int | None) -> None:
+        self._check(lib().epi_ensemble_set_stream(self._h, C.c_void_p(stream_ptr or 0)))
+
+    def set_profiling(self, on: bool) -> None:
+        self._check(lib().epi_ensemble_set_profiling(self._h, 1 if on else 0))
+
+    def kernel_stats(self) -> dict:
+        L = lib()
+        k = L.epi_engine_kernel_kinds()
+        launches = (C.c_uint32 * k)()
+        ms = (C.c_double * k)()
+        self._check(L.epi_ensemble_kernel_stats(self._h, launches, ms, k))
+        return {L.epi_engine_kernel_name(i).decode(): (launches[i], ms[i]) for i in range(k)}
+
+    def kernels_launched(self) -> int:
+        v = C.c_uint64(0)
+        self._check(lib().epi_ensemble_kernels_launched(self._h, C.byref(v)))
+        return v.value
+
+    def hour_bytes(self, hour: int) -> float:
+        b = C.c_double(0.0)
+        self._check(lib().epi_ensemble_hour_bytes(self._h, hour, C.byref(b)))
         return b.value

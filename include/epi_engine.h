@@ -265,6 +265,34 @@ size_t epi_abi_struct_size(const char* name);
 /* Algorithmic bytes of one hour at the current state (the roofline numerator). */
 int epi_engine_hour_bytes(const epi_engine* h, uint32_t hour, double* bytes);
 
+/* ---------------------------------------------------------------- batched ensemble */
+/* No counterpart in the reference (it runs one world per process; many runs mean many
+ * processes).  R independent worlds -- each with its own population, grid, disease, seed,
+ * hours and interventions -- share one device and advance together: every kernel of an hour
+ * serves all of them in one launch, hour segments are replayed as CUDA graphs.  Replicate r
+ * evolves exactly as a single engine created from params[r] would. */
+typedef struct epi_ensemble epi_ensemble;
+
+int epi_ensemble_create(const epi_params* params, uint32_t replicates, epi_ensemble** out);
+void epi_ensemble_destroy(epi_ensemble* e);
+const char* epi_ensemble_last_error(const epi_ensemble* e);
+int epi_ensemble_set_stream(epi_ensemble* e, void* cuda_stream);
+int epi_ensemble_replicates(const epi_ensemble* e, uint32_t* out);
+
+/* run_single_engine for every replicate (each with its own hours, interventions and stop
+ * rule).  rows[r * max_rows_per_replicate + k] gets hour k+1 of replicate r; n_rows[r] the
+ * number of rows of replicate r. */
+int epi_ensemble_run(epi_ensemble* e, epi_counts* rows, uint32_t max_rows_per_replicate, uint32_t* n_rows);
+
+int epi_ensemble_snapshot(epi_ensemble* e, uint32_t replicate, epi_agent_record* out, size_t n);
+int epi_ensemble_check(epi_ensemble* e);
+int epi_ensemble_save_state(epi_ensemble* e);
+int epi_ensemble_restore_state(epi_ensemble* e);
+int epi_ensemble_set_profiling(epi_ensemble* e, int on);
+int epi_ensemble_kernel_stats(const epi_ensemble* e, uint32_t* launches, double* total_ms, int n);
+int epi_ensemble_kernels_launched(const epi_ensemble* e, uint64_t* out);
+int epi_ensemble_hour_bytes(const epi_ensemble* e, uint32_t hour, double* bytes);
+
 /* ---------------------------------------------------------------- no-allocation hour */
 /* No counterpart in the reference.  One simulated hour (the work of epi_engine_simulate) on
  * device arrays that the caller owns, for callers that cannot allocate device memory: a host
