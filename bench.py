@@ -205,7 +205,32 @@ def run_batched(args, stream, flush) -> dict:
         ms_total += ev0.elapsed_time(ev1)
         agent_hours += sum(float(p.number_of_agents) * len(r) for p, r in zip(params, rows))
     ens.close()
-    return {"value": agent_hours / (ms_total / 1000.0), "unit": METRIC, "replicates": len(params), "agents": agents,
+    batched_value = agent_hours / (ms_total / 1000.0)
+
+    # the same replicates one at a time through the plain single-engine path (every 4th one,
+    # graphs warm: one untimed run per engine first)
+    from epirust_gb300 import Epidemiology
+
+    seq_ms, seq_ah = 0.0, 0.0
+    sample = params[::4]
+    for p in sample:
+        eng = Epidemiology(p)
+        eng.set_stream(stream.cuda_stream)
+        eng.save_state()
+        eng.run()
+        eng.restore_state()
+        ev0, ev1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        ev0.record(stream)
+        r = eng.run()
+        ev1.record(stream)
+        ev1.synchronize()
+        seq_ms += ev0.elapsed_time(ev1)
+        seq_ah += float(p.number_of_agents) * len(r)
+        eng.close()
+    sequential_value = seq_ah / (seq_ms / 1000.0)
+    return {"value": batched_value, "unit": METRIC, "replicates": len(params), "agents": agents,
+            "sequential_plain_value": sequential_value, "sequential_sample": len(sample),
+            "speedup_vs_sequential_plain": batched_value / sequential_value,
             "ms_per_step": ms_total / steps, "steps": steps, "world_build_and_upload_s": build_s,
             "workload": "256 replicates, populations log-uniform in [10k, 500k], grid ceil(sqrt(N/0.16)), regular "
                         "rate U[0.02, 0.10], 0.05% exposed, 2400 h, no interventions, seeds from 11"}

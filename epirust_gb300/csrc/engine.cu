@@ -68,7 +68,7 @@ struct epi_engine {
     uint32_t* h_hour_base = nullptr;
     cudaStream_t stream = nullptr;
     bool own_stream = false;
-    std::map<std::pair<uint32_t, uint32_t>, cudaGraphExec_t> graphs;  // (first hour mod 24, hours)
+    std::map<std::pair<uint32_t, uint32_t>, cudaGraphExec_t> graphs;  // (first hour mod 24 + 24 * window offset, hours)
     std::string err;
     bool profiling = false;
     uint32_t launches[kKindCount] = {};
@@ -76,6 +76,7 @@ struct epi_engine {
     std::vector<std::pair<int, std::pair<cudaEvent_t, cudaEvent_t>>> pending;
     std::vector<cudaEvent_t> event_pool;
     uint64_t kernels_launched = 0;
+    int64_t last_claim_hour = -1;  // latest hour whose claims may sit in the claim plane (-1: clean)
     // device-side checkpoint
     uint32_t *s_pos = nullptr, *s_wsa = nullptr;
     uint2* s_st = nullptr;
@@ -217,7 +218,34 @@ static int ensure_counts(epi_engine* h, uint32_t hours_needed) {
 }
 
 // ------------------------------------------------------------------ the hour loop
+using DecideKernel = void (*)(const DevParams*, const uint32_t*, uint32_t, const uint32_t*, uint2*, const uint32_t*,
+                              const uint32_t*, uint32_t*, const uint8_t*, uint32_t*, uint32_t*, uint32_t*,
+                              const uint32_t*, uint32_t, int*);
+
+// The k_decide instance of an hour of the day.
+static DecideKernel decide_kernel(uint32_t hod) {
+    switch (hour_class(hod)) {
+        case kHcStart: return k_decide<kHcStart>;
+        case kHcEnd: return k_decide<kHcEnd>;
+        case kHcTransport: return k_decide<kHcTransport>;
+        case kHcWork: return k_decide<kHcWork>;
+        case kHcNoon: return k_decide<kHcNoon>;
+        case kHcHome: return k_decide<kHcHome>;
+        default: return k_decide<kHcMove>;
+    }
+}
+
+static int commit_blocks_for(uint32_t slots) {
+    return (int)std::max<uint32_t>(1u, (slots + kThreads * kCommitSlots - 1) / (kThreads * kCommitSlots));
+}
 // Kernels of hours hour_base .. hour_base + nh - 1 (hour_base read on the device).
+// Offset within the segment of the first hour that opens a new claim window, or nh; later
+// windows open every kClaimWindow hours after it.
+static uint32_t window_start_offset(uint32_t first_hour, uint32_t nh) {
+    const uint32_t k = (kClaimWindow - first_hour % kClaimWindow) % kClaimWindow;
+    return (k > 0 && k < nh) ? k : nh;
+}
+
 static int enqueue_hours(epi_engine* h, uint32_t first_hour, uint32_t nh) {
     const size_t row_words = (size_t)h->R() * 8;
     CK(cudaMemsetAsync(h->d_counts, 0, (size_t)nh * row_words * sizeof(uint32_t), h->stream));
@@ -225,16 +253,18 @@ static int enqueue_hours(epi_engine* h, uint32_t first_hour, uint32_t nh) {
     for (uint32_t k = 0; k < nh; ++k) {
         const uint32_t hod = (first_hour + k) % 24u;
         uint32_t* rows = h->d_counts + (size_t)k * row_words;
+        if (k > 0 && (first_hour + k) % kClaimWindow == 0) CK(cudaMemsetAsync(h->d_claim, 0xFF, h->claim_cells * sizeof(uint32_t), h->stream));
         if (hod >= 1u && hod <= 6u) {
             LAUNCH(kKSleep, (k_sleep<<<h->grid_blocks, kThreads, 0, h->stream>>>(h->d_params, h->d_chunk_rep, n_chunks,
                                                                                   h->d_st, rows)));
         } else {
-            LAUNCH(kKDecide, (k_decide<<<h->grid_blocks, kThreads, 0, h->stream>>>(
+            const DecideKernel decide = decide_kernel(hod);
+            LAUNCH(kKDecide, (decide<<<h->grid_blocks, kThreads, 0, h->stream>>>(
                                   h->d_params, h->d_chunk_rep, n_chunks, h->d_pos, h->d_st, h->d_home, h->d_work, h->d_wsa,
                                   h->d_plane, h->d_claim, h->d_tgt, rows, h->d_hour_base, k, h->d_err)));
             LAUNCH(kKCommit, (k_commit<<<h->commit_blocks, kThreads, 0, h->stream>>>(h->d_params, h->d_chunk_rep, h->slots,
                                                                                      h->d_pos, h->d_tgt, h->d_plane,
-                                                                                     h->d_claim)));
+                                                                                     h->d_claim, h->d_hour_base, k)));
         }
     }
     CK(cudaMemcpyAsync(h->h_counts, h->d_counts, (size_t)nh * row_words * sizeof(uint32_t), cudaMemcpyDeviceToHost,
@@ -260,13 +290,19 @@ static int run_hours(epi_engine* h, uint32_t first_hour, uint32_t nh) {
     if ((uint64_t)first_hour + nh > 0xFFFFFFFFull) { h->err = "hour out of range"; return EPI_ERR_ARG; }
     int rc = ensure_counts(h, nh);
     if (rc) return rc;
+    // claims left by an earlier hour of another window, or by a later hour, must go first
+    if (h->last_claim_hour >= 0 &&
+        ((int64_t)first_hour <= h->last_claim_hour || first_hour / kClaimWindow != (uint64_t)h->last_claim_hour / kClaimWindow))
+        CK(cudaMemsetAsync(h->d_claim, 0xFF, h->claim_cells * sizeof(uint32_t), h->stream));
+    h->last_claim_hour = (int64_t)first_hour + nh - 1;
     *h->h_hour_base = first_hour;
     CK(cudaMemcpyAsync(h->d_hour_base, h->h_hour_base, sizeof(uint32_t), cudaMemcpyHostToDevice, h->stream));
     if (h->profiling) {
         rc = enqueue_hours(h, first_hour, nh);
         if (rc) return rc;
     } else {
-        auto key = std::make_pair(first_hour % 24u, nh);
+        // the kernel sequence depends on the hours of the day and on where a claim window opens
+        auto key = std::make_pair(first_hour % 24u + 24u * window_start_offset(first_hour, nh), nh);
         auto it = h->graphs.find(key);
         if (it == h->graphs.end()) {
             cudaGraph_t g;
@@ -536,11 +572,11 @@ static int engine_init(epi_engine* h, const epi_params* params, const epi_agent_
     int dev = 0, sms = 0, per_sm = 0;
     CK(cudaGetDevice(&dev));
     CK(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev));
-    CK(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_decide, kThreads, 0));
+    CK(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_decide<kHcMove>, kThreads, 0));
     per_sm = std::max(per_sm, 1);
     const uint64_t n_chunks = slots / kChunk;
     h->grid_blocks = (int)std::min<uint64_t>(n_chunks, (uint64_t)sms * per_sm);
-    h->commit_blocks = (int)n_chunks;
+    h->commit_blocks = commit_blocks_for(h->slots);
     CK(cudaStreamCreateWithFlags(&h->stream, cudaStreamNonBlocking));
     h->own_stream = true;
     CK(cudaMalloc(&h->d_params, R * sizeof(DevParams)));
@@ -670,9 +706,8 @@ static int check_all(epi_engine* h) {
     CK(cudaMemsetAsync(h->d_scratch, 0, 4 * sizeof(unsigned long long), h->stream));
     LAUNCH(kKCheck, (k_check_agents<<<blocks_for(h->slots), kThreads, 0, h->stream>>>(
                          h->d_params, h->d_chunk_rep, h->slots, h->d_pos, h->d_st, h->d_plane, h->d_scratch)));
-    LAUNCH(kKCheck, (k_check_plane<<<h->grid_blocks, kThreads, 0, h->stream>>>(h->plane_bytes, h->d_plane, h->claim_cells,
-                                                                                h->d_claim, h->d_scratch + 1,
-                                                                                h->d_scratch + 2)));
+    LAUNCH(kKCheck, (k_check_plane<<<h->grid_blocks, kThreads, 0, h->stream>>>(h->plane_bytes, h->d_plane,
+                                                                                h->d_scratch + 1)));
     unsigned long long v[4] = {0, 0, 0, 0};
     CK(cudaMemcpyAsync(v, h->d_scratch, sizeof v, cudaMemcpyDeviceToHost, h->stream));
     CK(cudaStreamSynchronize(h->stream));
@@ -680,9 +715,9 @@ static int check_all(epi_engine* h) {
     if (rc) return rc;
     uint64_t population = 0;
     for (const auto& rep : h->reps) population += rep.n;
-    if (v[0] || v[1] != population || v[2]) {
+    if (v[0] || v[1] != population) {
         h->err = "invariants: " + std::to_string(v[0]) + " agents off their cell class, " + std::to_string(v[1]) +
-                 " occupied cells for " + std::to_string(population) + " agents, " + std::to_string(v[2]) + " stale claims";
+                 " occupied cells for " + std::to_string(population) + " agents";
         return EPI_ERR_INVARIANT;
     }
     return EPI_OK;
@@ -719,6 +754,8 @@ static int restore_state(epi_engine* h) {
     CK(cudaMemcpyAsync(h->d_st, h->s_st, n * sizeof(uint2), cudaMemcpyDeviceToDevice, h->stream));
     CK(cudaMemcpyAsync(h->d_plane, h->s_plane, h->plane_bytes, cudaMemcpyDeviceToDevice, h->stream));
     CK(cudaMemsetAsync(h->d_tgt, 0xFF, n * sizeof(uint32_t), h->stream));
+    CK(cudaMemsetAsync(h->d_claim, 0xFF, h->claim_cells * sizeof(uint32_t), h->stream));
+    h->last_claim_hour = -1;
     for (auto& rep : h->reps) {
         rep.iv = rep.s_iv;
         rep.geo = rep.s_geo;
@@ -1123,7 +1160,7 @@ int noalloc_setup(int dev, NoAllocDevice** out) {
         NOALLOC_CK(cudaGetSymbolAddress(&ptr, g_noalloc_scratch));
         int sms = 0, per_sm = 0;
         NOALLOC_CK(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev));
-        NOALLOC_CK(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_decide, kThreads, 0));
+        NOALLOC_CK(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_decide<kHcMove>, kThreads, 0));
         d.grid_blocks = sms * std::max(per_sm, 1);
         d.base = static_cast<unsigned char*>(ptr);
     }
@@ -1177,9 +1214,10 @@ extern "C" int epi_tick_hour_noalloc(const epi_params* params, uint32_t hour, ui
         k_sleep<<<blocks, kThreads, 0, s>>>(d_params, nullptr, n_chunks, st, counts);
     } else {
         NOALLOC_CK(cudaMemsetAsync(d_claim, 0xFF, claim_bytes, s));
-        k_decide<<<blocks, kThreads, 0, s>>>(d_params, nullptr, n_chunks, pos, st, home, work, work_start_at, plane, d_claim,
-                                             d_tgt, counts, d_hour, 0u, d_err);
-        k_commit<<<(int)n_chunks, kThreads, 0, s>>>(d_params, nullptr, n, pos, d_tgt, plane, d_claim);
+        const DecideKernel decide = decide_kernel(hod);
+        decide<<<blocks, kThreads, 0, s>>>(d_params, nullptr, n_chunks, pos, st, home, work, work_start_at, plane, d_claim,
+                                           d_tgt, counts, d_hour, 0u, d_err);
+        k_commit<<<commit_blocks_for(n), kThreads, 0, s>>>(d_params, nullptr, n, pos, d_tgt, plane, d_claim, d_hour, 0u);
     }
     NOALLOC_CK(cudaGetLastError());
     int err = 0;

@@ -46,7 +46,17 @@ constexpr uint32_t kDayMask = 0xFFFFu << kDayShift;
 enum AreaCode : uint32_t { kHome = 0, kWork = 1, kTransport = 2, kHousing = 3, kHosp0 = 4, kHosp1 = 5, kNumAreas = 6 };
 
 constexpr uint32_t kNoAction = 0xFFFFFFFFu;  // tgt[i]: nothing to commit
-constexpr uint32_t kNoClaim = 0xFFFFFFFFu;   // claim plane: free
+constexpr uint32_t kNoClaim = 0xFFFFFFFFu;   // claim plane: free (larger than any key)
+// Claim keys: (127 - hour mod 128) << 25 | agent.  Within a window of 128 hours that starts
+// at a multiple of 128 a later hour has a smaller key, so atomicMin lets this hour's claims
+// replace stale ones and the lowest agent index win among them; the plane is cleared at the
+// start of every window and after any rewind of the hour.
+constexpr uint32_t kClaimAgentBits = 25;
+constexpr uint32_t kMaxAgentsPerWorld = (1u << kClaimAgentBits) - 1u;  // 33,554,431
+constexpr uint32_t kClaimWindow = 128;
+EPI_HD uint32_t claim_key(uint32_t hour, uint32_t agent) {
+    return ((kClaimWindow - 1u - (hour & (kClaimWindow - 1u))) << kClaimAgentBits) | agent;
+}
 constexpr uint32_t kWorldHour = 0xFFFFFFFFu; // Philox counter word 1 of world-build draws
 constexpr uint32_t kMaxHours = 1500000u;     // infection day fits 16 bits
 

@@ -12,8 +12,8 @@
 //   hours 1..6 of a day   k_sleep   current_area = home (non-staff), counts
 //   other hours           k_decide  per-agent rules on the previous-hour plane, proposals,
 //                                   atomicMin claims on the target cells, counts
-//                         k_commit  lowest claimant moves, losers stay, plane bytes updated,
-//                                   claims released
+//                         k_commit  lowest claimant moves, losers stay, plane bytes updated;
+//                                   claims stay (a later hour's keys are smaller, see claim_key)
 #pragma once
 
 #include "tick.cuh"
@@ -23,13 +23,17 @@ namespace kern {
 
 constexpr int kThreads = (int)kChunk;
 
-// Warp-aggregated 6-bin histogram into shared memory.
+// Warp-aggregated 6-bin histogram into shared memory: three ballots carry the bits of each
+// lane's bin (invalid lanes vote bin 7), and lane b (< 6) counts the lanes whose bits spell b.
 __device__ __forceinline__ void count_into(uint32_t* sh, bool valid, uint32_t bin) {
-    const int lane = threadIdx.x & 31;
-#pragma unroll
-    for (uint32_t b = 0; b < 6; ++b) {
-        uint32_t c = __popc(__ballot_sync(0xFFFFFFFFu, valid && bin == b));
-        if (lane == 0 && c) atomicAdd(&sh[b], c);
+    const uint32_t v = valid ? bin : 7u;
+    const uint32_t b0 = __ballot_sync(0xFFFFFFFFu, v & 1u), b1 = __ballot_sync(0xFFFFFFFFu, v & 2u),
+                   b2 = __ballot_sync(0xFFFFFFFFu, v & 4u);
+    const uint32_t lane = threadIdx.x & 31u;
+    if (lane < 6u) {
+        const uint32_t m = ((lane & 1u) ? b0 : ~b0) & ((lane & 2u) ? b1 : ~b1) & ((lane & 4u) ? b2 : ~b2);
+        const uint32_t c = (uint32_t)__popc(m);
+        if (c) atomicAdd(&sh[lane], c);
     }
 }
 
@@ -103,7 +107,8 @@ __global__ void __launch_bounds__(kThreads) k_sleep(const DevParams* __restrict_
     flush_rep(br, sh, counts);
 }
 
-// One hour of per-agent rules (hour of day 0, 7..22 or 23).
+// One hour of per-agent rules (hour of day 0, 7..22 or 23), specialised per hour class HC.
+template <int HC>
 __global__ void __launch_bounds__(kThreads) k_decide(const DevParams* __restrict__ Pall, const uint32_t* __restrict__ chunk_rep,
                                                      uint32_t n_chunks, const uint32_t* __restrict__ pos,
                                                      uint2* __restrict__ st, const uint32_t* __restrict__ home,
@@ -139,7 +144,7 @@ __global__ void __launch_bounds__(kThreads) k_decide(const DevParams* __restrict
             at = sv.y;
             p = pos[slot];
         }
-        if (hod == 0u) {
+        if (HC == kHcStart) {
             const bool need = valid && wants_hospital(P, infected(s) ? with_day(s, st_day(s) + 1u) : s);
             if (__syncthreads_or(need) && !hosp_known) {
                 hosp_first = block_first_vacant(P, pl);
@@ -153,14 +158,14 @@ __global__ void __launch_bounds__(kThreads) k_decide(const DevParams* __restrict
             const Cell cell{unpack_x(p), unpack_y(p)};
             Draws dr{i, hour, P.key0, P.key1};
             Cell nc;
-            if (hod == 0u) {
+            if (HC == kHcStart) {
                 nc = routine_start(P, pl, s, hm, cell, hosp_first, dr);
-            } else if (hod == 23u) {
+            } else if (HC == kHcEnd) {
                 nc = routine_end(P, pl, s, hm, cell, dr);
             } else {
                 const bool staff = st_ws(s) == EPI_WS_HOSPITAL_STAFF;
                 uint32_t w0 = staff ? wsa[slot] : 0u, w = w0;
-                nc = perform_movements(P, pl, s, at, w, hm, wk, cell, hod, hour, dr);
+                nc = perform_movements<HC>(P, pl, s, at, w, hm, wk, cell, hod, hour, dr);
                 if (staff && w != w0) wsa[slot] = w;
             }
             bool moving = nc.x != cell.x || nc.y != cell.y;
@@ -170,7 +175,7 @@ __global__ void __launch_bounds__(kThreads) k_decide(const DevParams* __restrict
                 nc = cell;
             }
             const uint32_t cls = cell_class(P, s);
-            if (moving) atomicMin(&rclaim[(size_t)nc.y * P.W + nc.x], i);
+            if (moving) atomicMin(&rclaim[(size_t)nc.y * P.W + nc.x], claim_key(hour, i));
             tgt[slot] = (moving || cls != cell_class(P, s0)) ? encode_target(nc, cls) : kNoAction;
             if (s != s0 || at != at0) st[slot] = make_uint2(s, at);
             bin = count_bin(s);
@@ -182,34 +187,54 @@ __global__ void __launch_bounds__(kThreads) k_decide(const DevParams* __restrict
 
 // Resolve the claims of the hour: the lowest index that claimed a cell moves there
 // (the serial resolve of allocation_map.rs:93-102 in index order), others keep their cell.
+// Each thread takes kCommitSlots slots a block-width apart, issuing all their independent
+// loads before the dependent claim reads.
+constexpr int kCommitSlots = 4;
+
 __global__ void __launch_bounds__(kThreads) k_commit(const DevParams* __restrict__ Pall, const uint32_t* __restrict__ chunk_rep,
                                                      uint32_t n_slots, uint32_t* __restrict__ pos,
                                                      const uint32_t* __restrict__ tgt, uint8_t* __restrict__ plane,
-                                                     uint32_t* __restrict__ claim) {
-    const uint32_t stride = gridDim.x * blockDim.x;
-    for (uint32_t slot = blockIdx.x * blockDim.x + threadIdx.x; slot < n_slots; slot += stride) {
-        const uint32_t t = tgt[slot];
-        if (t == kNoAction) continue;
-        const DevParams* Pr = Pall + (chunk_rep ? chunk_rep[slot / kChunk] : 0u);
-        if (!Pr->active) continue;
-        const uint32_t W = (uint32_t)Pr->W, WP = (uint32_t)Pr->WP;
-        uint8_t* rplane = plane + Pr->plane_off;
-        uint32_t* rclaim = claim + Pr->claim_off;
-        const uint32_t i = slot - Pr->agent_off;
-        const uint32_t p = pos[slot];
-        const uint32_t xy = target_xy(t), cls = target_class(t);
-        const size_t old_cell = (size_t)(unpack_y(p) + 1) * WP + (unpack_x(p) + 1);
-        if (xy != p) {
-            const size_t claim_cell = (size_t)unpack_y(xy) * W + unpack_x(xy);
-            if (rclaim[claim_cell] == i) {
-                rclaim[claim_cell] = kNoClaim;
-                rplane[old_cell] = 0;
-                rplane[(size_t)(unpack_y(xy) + 1) * WP + (unpack_x(xy) + 1)] = (uint8_t)cls;
-                pos[slot] = xy;
-                continue;
-            }
+                                                     const uint32_t* __restrict__ claim,
+                                                     const uint32_t* __restrict__ hour_base, uint32_t hour_offset) {
+    const uint32_t hour = *hour_base + hour_offset;
+    const uint32_t base = blockIdx.x * (blockDim.x * kCommitSlots) + threadIdx.x;
+    uint32_t t[kCommitSlots], p[kCommitSlots];
+#pragma unroll
+    for (int k = 0; k < kCommitSlots; ++k) {
+        const uint32_t slot = base + k * blockDim.x;
+        t[k] = slot < n_slots ? tgt[slot] : kNoAction;
+        p[k] = slot < n_slots ? pos[slot] : 0u;
+    }
+    const DevParams* Pr[kCommitSlots];
+    uint32_t won[kCommitSlots];
+#pragma unroll
+    for (int k = 0; k < kCommitSlots; ++k) {
+        const uint32_t slot = base + k * blockDim.x;
+        Pr[k] = Pall + (chunk_rep && t[k] != kNoAction ? chunk_rep[slot / kChunk] : 0u);
+        won[k] = kNoClaim;  // no claim read: never equal to a key
+        if (t[k] != kNoAction && target_xy(t[k]) != p[k]) {
+            const uint32_t xy = target_xy(t[k]);
+            won[k] = claim[Pr[k]->claim_off + (size_t)unpack_y(xy) * (uint32_t)Pr[k]->W + unpack_x(xy)];
         }
-        rplane[old_cell] = (uint8_t)cls;
+    }
+#pragma unroll
+    for (int k = 0; k < kCommitSlots; ++k) {
+        if (t[k] == kNoAction) continue;
+        const DevParams& P = *Pr[k];
+        if (!P.active) continue;
+        const uint32_t slot = base + k * blockDim.x;
+        const uint32_t i = slot - P.agent_off;
+        const uint32_t WP = (uint32_t)P.WP;
+        uint8_t* rplane = plane + P.plane_off;
+        const uint32_t xy = target_xy(t[k]), cls = target_class(t[k]);
+        const size_t old_cell = (size_t)(unpack_y(p[k]) + 1) * WP + (unpack_x(p[k]) + 1);
+        if (won[k] == claim_key(hour, i)) {
+            rplane[old_cell] = 0;
+            rplane[(size_t)(unpack_y(xy) + 1) * WP + (unpack_x(xy) + 1)] = (uint8_t)cls;
+            pos[slot] = xy;
+        } else {
+            rplane[old_cell] = (uint8_t)cls;
+        }
     }
 }
 
@@ -262,22 +287,13 @@ __global__ void k_check_agents(const DevParams* __restrict__ Pall, const uint32_
     }
 }
 
-// Occupied plane bytes and taken claims over the whole buffers.
-__global__ void k_check_plane(size_t plane_bytes, const uint8_t* __restrict__ plane, size_t claim_cells,
-                              const uint32_t* __restrict__ claim, unsigned long long* occupied,
-                              unsigned long long* claimed) {
-    unsigned long long o = 0, c = 0;
+// Occupied plane bytes over the whole buffer (borders and slack included: they must be 0).
+__global__ void k_check_plane(size_t plane_bytes, const uint8_t* __restrict__ plane, unsigned long long* occupied) {
+    unsigned long long o = 0;
     const size_t stride = (size_t)gridDim.x * blockDim.x;
     for (size_t k = blockIdx.x * (size_t)blockDim.x + threadIdx.x; k < plane_bytes; k += stride) o += plane[k] != 0;
-    for (size_t k = blockIdx.x * (size_t)blockDim.x + threadIdx.x; k < claim_cells; k += stride) c += claim[k] != kNoClaim;
-    for (int off = 16; off; off >>= 1) {
-        o += __shfl_down_sync(0xFFFFFFFFu, o, off);
-        c += __shfl_down_sync(0xFFFFFFFFu, c, off);
-    }
-    if ((threadIdx.x & 31) == 0) {
-        if (o) atomicAdd(occupied, o);
-        if (c) atomicAdd(claimed, c);
-    }
+    for (int off = 16; off; off >>= 1) o += __shfl_down_sync(0xFFFFFFFFu, o, off);
+    if ((threadIdx.x & 31) == 0 && o) atomicAdd(occupied, o);
 }
 
 }  // namespace kern

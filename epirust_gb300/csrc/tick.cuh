@@ -51,30 +51,39 @@ struct PlaneView {
     }
 };
 
-// 8-bit masks of the Moore neighbourhood of one cell.
-struct Nbhd {
-    uint32_t occupied, infectious, high;
-};
-
 // Gather the per-byte flag bits (bits 0, 8, 16 of each row) into NeighborIterator order.
 __device__ __forceinline__ uint32_t gather8(uint32_t f0, uint32_t f1, uint32_t f2) {
     return (f0 & 1u) | ((f0 >> 7) & 2u) | ((f0 >> 14) & 4u) | ((f1 & 1u) << 3) | ((f1 >> 12) & 16u) |
            ((f2 & 1u) << 5) | ((f2 >> 2) & 64u) | ((f2 >> 9) & 128u);
 }
 
-// Plane bytes are 0..3: occupied <=> bit0|bit1, infectious <=> bit1, high rate <=> bit0&bit1.
-__device__ __forceinline__ Nbhd neighbourhood(const PlaneView& pl, int32_t x, int32_t y) {
+// The three rows of the 3x3 block around (x, y); a cell outside [0, G]^2 reads as a
+// block of occupied, non-infectious cells (and is reported).
+struct Rows3 {
+    uint32_t r0, r1, r2;
+};
+__device__ __forceinline__ Rows3 rows_around(const PlaneView& pl, int32_t x, int32_t y) {
     if (!pl.inside(x, y)) {
         atomicOr(pl.err, 1);
-        return Nbhd{0xFFu, 0u, 0u};
+        return Rows3{0x010101u, 0x010101u, 0x010101u};
     }
-    const uint32_t r0 = pl.row3(x, y - 1), r1 = pl.row3(x, y), r2 = pl.row3(x, y + 1);
+    return Rows3{pl.row3(x, y - 1), pl.row3(x, y), pl.row3(x, y + 1)};
+}
+
+// Plane bytes are 0..3: occupied <=> bit0|bit1, infectious <=> bit1, high rate <=> bit0&bit1.
+__device__ __forceinline__ uint32_t occupied_mask(const Rows3& r) {
     const uint32_t m = 0x010101u;
-    Nbhd n;
-    n.occupied = gather8((r0 | (r0 >> 1)) & m, (r1 | (r1 >> 1)) & m, (r2 | (r2 >> 1)) & m);
-    n.infectious = gather8((r0 >> 1) & m, (r1 >> 1) & m, (r2 >> 1) & m);
-    n.high = gather8(r0 & (r0 >> 1) & m, r1 & (r1 >> 1) & m, r2 & (r2 >> 1) & m);
-    return n;
+    return gather8((r.r0 | (r.r0 >> 1)) & m, (r.r1 | (r.r1 >> 1)) & m, (r.r2 | (r.r2 >> 1)) & m);
+}
+// Any infectious byte among the nine (the centre is vacant or the agent's own, never infectious).
+__device__ __forceinline__ bool any_infectious(const Rows3& r) { return ((r.r0 | r.r1 | r.r2) & 0x020202u) != 0u; }
+__device__ __forceinline__ uint32_t infectious_mask(const Rows3& r) {
+    const uint32_t m = 0x010101u;
+    return gather8((r.r0 >> 1) & m, (r.r1 >> 1) & m, (r.r2 >> 1) & m);
+}
+__device__ __forceinline__ uint32_t high_mask(const Rows3& r) {
+    const uint32_t m = 0x010101u;
+    return gather8(r.r0 & (r.r0 >> 1) & m, r.r1 & (r.r1 >> 1) & m, r.r2 & (r.r2 >> 1) & m);
 }
 
 // Neighbours of (x, y) inside area a and the grid (Area::get_neighbors_of filtered by
@@ -85,6 +94,17 @@ __device__ __forceinline__ uint32_t valid_neighbours(const Rect& a, int32_t G, i
     const uint32_t rt = (y - 1 >= ly) & (y - 1 <= hy), rm = (y >= ly) & (y <= hy), rb = (y + 1 >= ly) & (y + 1 <= hy);
     return (cl & rt) | ((cc & rt) << 1) | ((cr & rt) << 2) | ((cl & rm) << 3) | ((cr & rm) << 4) | ((cl & rb) << 5) |
            ((cc & rb) << 6) | ((cr & rb) << 7);
+}
+
+// Position of the j-th set bit (j counted from 0, j < popc(m)) of an 8-bit mask.
+__device__ __forceinline__ int nth_set_bit8(uint32_t m, uint32_t j) {
+    int base = 0;
+    const uint32_t c4 = (uint32_t)__popc(m & 0xFu);
+    if (j >= c4) { j -= c4; m >>= 4; base = 4; }
+    const uint32_t c2 = (uint32_t)__popc(m & 0x3u);
+    if (j >= c2) { j -= c2; m >>= 2; base += 2; }
+    if (j >= (m & 1u)) base += 1;
+    return base;
 }
 
 // Lazily materialised Philox blocks of one agent-hour.
@@ -148,10 +168,10 @@ __device__ __forceinline__ Cell move_agent_from(const PlaneView& pl, uint32_t s,
     if (!can_move(s)) return cell;
     Cell c = cell;
     if (!rect_has(cur, cell.x, cell.y)) c = random_point(cur, dr.m(0), dr.m(1));
-    const uint32_t cand = valid_neighbours(cur, pl.G, c.x, c.y) & ~neighbourhood(pl, c.x, c.y).occupied;
+    const uint32_t cand = valid_neighbours(cur, pl.G, c.x, c.y) & ~occupied_mask(rows_around(pl, c.x, c.y));
     if (!cand) return cell;
     const uint32_t j = uniform_index(dr.m(2), (uint32_t)__popc(cand));
-    const int k = (int)__fns(cand, 0u, (int)j + 1);  // position of the j-th set bit
+    const int k = nth_set_bit8(cand, j);
     return Cell{c.x + nb_dx(k), c.y + nb_dy(k)};     // vacant by construction: move_agent keeps it
 }
 
@@ -180,16 +200,18 @@ __device__ __forceinline__ void infection_dynamics(const DevParams& P, const Pla
     const uint32_t v = s & kStateMask;
     if (v == EPI_S) {
         if (s & (kWq | kVacc)) return;
-        const Nbhd nb = neighbourhood(pl, cell.x, cell.y);
-        uint32_t cand = valid_neighbours(cur, pl.G, cell.x, cell.y) & nb.infectious;
-        if (!cand) return;  // no infectious occupant among the neighbours: no draw can succeed
+        const Rows3 rows = rows_around(pl, cell.x, cell.y);
+        if (!any_infectious(rows)) return;  // no infectious neighbour: no draw can succeed
+        const uint32_t cand = valid_neighbours(cur, pl.G, cell.x, cell.y) & infectious_mask(rows);
+        if (!cand) return;
+        const uint32_t high = high_mask(rows);
         const uint64_t thr_reg = P.thr_rate[1], thr_high = P.thr_rate[2];
         // neighbours in NeighborIterator order; the first successful Bernoulli exposes
 #pragma unroll
         for (int k = 0; k < 8; ++k) {
             if (!((cand >> k) & 1u)) continue;
             const uint32_t u = k < 4 ? dr.d(k) : dr.d2(k - 4);
-            if ((uint64_t)u < (((nb.high >> k) & 1u) ? thr_high : thr_reg)) {
+            if ((uint64_t)u < (((high >> k) & 1u) ? thr_high : thr_reg)) {
                 s = with_state(s, EPI_E);
                 at = hour;
                 return;
@@ -210,64 +232,108 @@ __device__ __forceinline__ void infection_dynamics(const DevParams& P, const Pla
     }
 }
 
-// Citizen::perform_movements, citizen/mod.rs:257-349 (hours 7..22 of the day).
+// Hour-of-day classes of the routine (constants.rs:27-36); the kernels are specialised per
+// class so that each launch carries only the branches its hour can take.
+enum HourClass : int {
+    kHcStart = 0,     // 0: ROUTINE_START_TIME
+    kHcEnd = 1,       // 23: ROUTINE_END_TIME
+    kHcMove = 2,      // 9-11, 13-15, 18-22: everyone but hospital staff walks (move_agent_from)
+    kHcTransport = 3, // 7, 17: ROUTINE_TRAVEL_START/END_TIME
+    kHcWork = 4,      // 8: ROUTINE_WORK_TIME
+    kHcNoon = 5,      // 12: NON_WORKING_TRAVEL_END_TIME
+    kHcHome = 6,      // 16: ROUTINE_WORK_END_TIME
+    kHcSleep = 7      // 1-6: SLEEP_START_TIME..=SLEEP_END_TIME
+};
+
+__host__ __device__ constexpr int hour_class(uint32_t hod) {
+    return hod == 0u ? kHcStart
+         : hod == 23u ? kHcEnd
+         : (hod >= 1u && hod <= 6u) ? kHcSleep
+         : (hod == 7u || hod == 17u) ? kHcTransport
+         : hod == 8u ? kHcWork
+         : hod == 12u ? kHcNoon
+         : hod == 16u ? kHcHome
+         : kHcMove;
+}
+
+// The HospitalStaff arm of Citizen::perform_movements (citizen/mod.rs:292-328).  Returns
+// false when the hour ends before the infection update (the two early returns).
+__device__ __forceinline__ bool staff_movements(const DevParams& P, const PlaneView& pl, uint32_t& s, uint32_t& wsa,
+                                                uint32_t home, uint32_t work, Cell cell, Cell& nc, uint32_t hod,
+                                                uint32_t hour, Draws& dr) {
+    const Rect cur = area_rect(P, st_area(s), home, work);
+    const uint32_t since = hour >= wsa ? hour - wsa : 0u;  // saturating_sub
+    if (since == 24u * 14u) {
+        s |= kWq;
+        return false;
+    }
+    if (since == 24u * 14u * 2u) {
+        nc = goto_area(pl, s, cur, home_rect(home), home, work, cell, dr);
+        s = with_area(s, kHome);
+        wsa = hour + 24u * 14u;
+        return false;
+    }
+    if (hod == 8u) {
+        const Rect hosp = P.area[P.hosp_code];
+        if (!rect_eq(cur, hosp) && wsa <= hour) {
+            nc = goto_area(pl, s, cur, hosp, home, work, cell, dr);
+            s = with_area(s, P.hosp_code);
+            wsa = hour;
+        }
+        s &= ~kWq;
+    } else if (hod == 16u) {
+        s |= kWq;
+    } else if (!(s & kWq) && can_move(s)) {
+        nc = move_agent_from(pl, s, cur, cell, dr);
+    }
+    return true;
+}
+
+// Citizen::perform_movements, citizen/mod.rs:257-349, for the movement classes (hours 7..22):
+// the work-status arms (Normal|Essential, HospitalStaff, NA) at hour class HC, then the
+// infection update of DiseaseStateMachine::next.
+template <int HC>
 __device__ __forceinline__ Cell perform_movements(const DevParams& P, const PlaneView& pl, uint32_t& s, uint32_t& at,
                                                   uint32_t& wsa, uint32_t home, uint32_t work, Cell cell,
                                                   uint32_t hod, uint32_t hour, Draws& dr) {
     const uint32_t ws = st_ws(s);
     Cell nc = cell;
-    Rect cur = area_rect(P, st_area(s), home, work);
-    if (ws == EPI_WS_NORMAL || ws == EPI_WS_ESSENTIAL) {
-        if (hod == 7u || hod == 17u) {
-            if (s & kPt) {
+    if (ws == EPI_WS_HOSPITAL_STAFF) {
+        if (!staff_movements(P, pl, s, wsa, home, work, cell, nc, hod, hour, dr)) return nc;
+    } else {
+        const Rect cur = area_rect(P, st_area(s), home, work);
+        const bool worker = ws != EPI_WS_NA;  // Normal or Essential here
+        if (HC == kHcMove) {
+            nc = move_agent_from(pl, s, cur, cell, dr);
+        } else if (HC == kHcTransport) {
+            if (worker && (s & kPt)) {
                 nc = goto_area(pl, s, cur, P.area[kTransport], home, work, cell, dr);
                 s = with_area(s, kTransport);
             } else {
                 nc = move_agent_from(pl, s, cur, cell, dr);
             }
-        } else if (hod == 8u) {
-            nc = goto_area(pl, s, cur, office_rect(work), home, work, cell, dr);
-            s = with_area(s, kWork);
-        } else if (hod == 16u) {
-            nc = goto_area(pl, s, cur, home_rect(home), home, work, cell, dr);
-            s = with_area(s, kHome);
-        } else {
-            nc = move_agent_from(pl, s, cur, cell, dr);
-        }
-    } else if (ws == EPI_WS_HOSPITAL_STAFF) {
-        const uint32_t since = hour >= wsa ? hour - wsa : 0u;  // saturating_sub
-        if (since == 24u * 14u) {
-            s |= kWq;
-            return nc;
-        }
-        if (since == 24u * 14u * 2u) {
-            nc = goto_area(pl, s, cur, home_rect(home), home, work, cell, dr);
-            s = with_area(s, kHome);
-            wsa = hour + 24u * 14u;
-            return nc;
-        }
-        if (hod == 8u) {
-            const Rect hosp = P.area[P.hosp_code];
-            if (!rect_eq(cur, hosp) && wsa <= hour) {
-                nc = goto_area(pl, s, cur, hosp, home, work, cell, dr);
-                s = with_area(s, P.hosp_code);
-                wsa = hour;
+        } else if (HC == kHcWork) {
+            if (worker) {
+                nc = goto_area(pl, s, cur, office_rect(work), home, work, cell, dr);
+                s = with_area(s, kWork);
+            } else {
+                nc = goto_area(pl, s, cur, P.area[kHousing], home, work, cell, dr);
+                s = with_area(s, kHousing);
             }
-            s &= ~kWq;
-        } else if (hod == 16u) {
-            s |= kWq;
-        } else if (!(s & kWq) && can_move(s)) {
-            nc = move_agent_from(pl, s, cur, cell, dr);
-        }
-    } else {  // NA
-        if (hod == 8u) {
-            nc = goto_area(pl, s, cur, P.area[kHousing], home, work, cell, dr);
-            s = with_area(s, kHousing);
-        } else if (hod == 12u) {
-            nc = goto_area(pl, s, cur, home_rect(home), home, work, cell, dr);
-            s = with_area(s, kHome);
-        } else {
-            nc = move_agent_from(pl, s, cur, cell, dr);
+        } else if (HC == kHcNoon) {
+            if (worker) {
+                nc = move_agent_from(pl, s, cur, cell, dr);
+            } else {
+                nc = goto_area(pl, s, cur, home_rect(home), home, work, cell, dr);
+                s = with_area(s, kHome);
+            }
+        } else {  // kHcHome
+            if (worker) {
+                nc = goto_area(pl, s, cur, home_rect(home), home, work, cell, dr);
+                s = with_area(s, kHome);
+            } else {
+                nc = move_agent_from(pl, s, cur, cell, dr);
+            }
         }
     }
     infection_dynamics(P, pl, s, at, area_rect(P, st_area(s), home, work), nc, hour, dr);

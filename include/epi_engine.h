@@ -236,8 +236,8 @@ int epi_engine_snapshot(epi_engine* h, epi_agent_record* out, size_t n);
 /* Current geography (the hospital changes after BuildNewHospital). */
 int epi_engine_geography(const epi_engine* h, epi_geography* out);
 
-/* Check the device invariants: every agent sits on its own plane cell, the plane holds
- * exactly population occupied cells and the claim plane is clear. */
+/* Check the device invariants: every agent sits on its own plane cell and the plane holds
+ * exactly population occupied cells. */
 int epi_engine_check(epi_engine* h);
 
 /* Device-side checkpoint of the agent state, the plane, the intervention state and the
