@@ -16,6 +16,7 @@
 #include <mutex>
 #include <string>
 #include <thread>
+#include <tuple>
 #include <utility>
 #include <vector>
 
@@ -27,6 +28,13 @@ using namespace epi::kern;
 
 enum KernelKind { kKDecide = 0, kKCommit, kKSleep, kKLock, kKVaccinate, kKBuildPlane, kKCheck, kKindCount };
 static const char* kKernelNames[kKindCount] = {"k_decide", "k_commit", "k_sleep", "k_lock", "k_vaccinate", "k_build_plane", "k_check"};
+
+// A timed kernel launch: its kind and the events recorded around it.
+struct TimedLaunch {
+    int kind;
+    cudaEvent_t begin, end;
+    bool pooled;  // the pair returns to the engine's pool once read
+};
 
 // One world on the device.
 struct Replica {
@@ -55,6 +63,7 @@ struct epi_engine {
     DevParams* d_params = nullptr;
     uint32_t* d_chunk_rep = nullptr;  // null for a single replicate
     uint32_t *d_pos = nullptr, *d_home = nullptr, *d_work = nullptr, *d_wsa = nullptr, *d_tgt = nullptr;
+    uint32_t* d_lost = nullptr;  // per slot: the hour in which the agent's claim was beaten
     uint2* d_st = nullptr;
     uint8_t* d_plane = nullptr;
     uint32_t* d_claim = nullptr;
@@ -68,13 +77,20 @@ struct epi_engine {
     uint32_t* h_hour_base = nullptr;
     cudaStream_t stream = nullptr;
     bool own_stream = false;
-    std::map<std::pair<uint32_t, uint32_t>, cudaGraphExec_t> graphs;  // (first hour mod 24 + 24 * window offset, hours)
+    // hour graphs by (first hour mod 24 + 24 * window offset, hours, profiling); a profiling
+    // graph carries an event-record node before and after each kernel
+    struct HourGraph {
+        cudaGraphExec_t exec = nullptr;
+        std::vector<TimedLaunch> events;
+    };
+    std::map<std::tuple<uint32_t, uint32_t, bool>, HourGraph> graphs;
     std::string err;
     bool profiling = false;
     uint32_t launches[kKindCount] = {};
     double total_ms[kKindCount] = {};
-    std::vector<std::pair<int, std::pair<cudaEvent_t, cudaEvent_t>>> pending;
+    std::vector<TimedLaunch> pending;          // launches whose events are not read yet
     std::vector<cudaEvent_t> event_pool;
+    std::vector<TimedLaunch>* capture = nullptr;  // set while a profiling graph is captured
     uint64_t kernels_launched = 0;
     int64_t last_claim_hour = -1;  // latest hour whose claims may sit in the claim plane (-1: clean)
     // device-side checkpoint
@@ -147,39 +163,61 @@ static uint32_t area_code_of(const DevParams& hp, const epi_agent_record& r, boo
 }
 
 // ------------------------------------------------------------------ launch bookkeeping
+// Eagerly launched kernels take their event pair from the pool and return it once read;
+// kernels captured into a profiling graph get a pair of their own, recorded as external
+// event nodes, which the graph keeps and re-records at every replay.
 static int record_launch_begin(epi_engine* h, int kind, cudaEvent_t* out_end) {
     if (!h->profiling) return EPI_OK;
     cudaEvent_t a, b;
-    if (h->event_pool.size() >= 2) {
-        a = h->event_pool.back(); h->event_pool.pop_back();
-        b = h->event_pool.back(); h->event_pool.pop_back();
-    } else {
+    if (h->capture) {
         CK(cudaEventCreate(&a));
         CK(cudaEventCreate(&b));
+        CK(cudaEventRecordWithFlags(a, h->stream, cudaEventRecordExternal));
+        h->capture->push_back({kind, a, b, false});
+    } else {
+        if (h->event_pool.size() >= 2) {
+            a = h->event_pool.back(); h->event_pool.pop_back();
+            b = h->event_pool.back(); h->event_pool.pop_back();
+        } else {
+            CK(cudaEventCreate(&a));
+            CK(cudaEventCreate(&b));
+        }
+        CK(cudaEventRecord(a, h->stream));
+        h->pending.push_back({kind, a, b, true});
     }
-    CK(cudaEventRecord(a, h->stream));
-    h->pending.push_back({kind, {a, b}});
     *out_end = b;
     return EPI_OK;
 }
 
 static int record_launch_end(epi_engine* h, cudaEvent_t end) {
     if (!h->profiling) return EPI_OK;
-    CK(cudaEventRecord(end, h->stream));
+    if (h->capture) CK(cudaEventRecordWithFlags(end, h->stream, cudaEventRecordExternal));
+    else CK(cudaEventRecord(end, h->stream));
     return EPI_OK;
 }
 
+// Read the pending launches' durations (the stream has been synchronised).
 static int harvest_events(epi_engine* h) {
     for (auto& pe : h->pending) {
         float ms = 0.f;
-        CK(cudaEventElapsedTime(&ms, pe.second.first, pe.second.second));
-        h->launches[pe.first]++;
-        h->total_ms[pe.first] += ms;
-        h->event_pool.push_back(pe.second.first);
-        h->event_pool.push_back(pe.second.second);
+        CK(cudaEventElapsedTime(&ms, pe.begin, pe.end));
+        h->launches[pe.kind]++;
+        h->total_ms[pe.kind] += ms;
+        if (pe.pooled) {
+            h->event_pool.push_back(pe.begin);
+            h->event_pool.push_back(pe.end);
+        }
     }
     h->pending.clear();
     return EPI_OK;
+}
+
+static void destroy_graphs(epi_engine* h) {
+    for (auto& g : h->graphs) {
+        cudaGraphExecDestroy(g.second.exec);
+        for (auto& t : g.second.events) { cudaEventDestroy(t.begin); cudaEventDestroy(t.end); }
+    }
+    h->graphs.clear();
 }
 
 #define LAUNCH(kind, ...)                                                                    \
@@ -212,15 +250,23 @@ static int ensure_counts(epi_engine* h, uint32_t hours_needed) {
     CK(cudaMalloc(&h->d_counts, words * sizeof(uint32_t)));
     CK(cudaMallocHost(&h->h_counts, words * sizeof(uint32_t)));
     h->counts_capacity = cap;
-    for (auto& g : h->graphs) cudaGraphExecDestroy(g.second);  // they reference the old buffer
-    h->graphs.clear();
+    destroy_graphs(h);  // they reference the old buffer
     return EPI_OK;
 }
 
 // ------------------------------------------------------------------ the hour loop
 using DecideKernel = void (*)(const DevParams*, const uint32_t*, uint32_t, const uint32_t*, uint2*, const uint32_t*,
-                              const uint32_t*, uint32_t*, const uint8_t*, uint32_t*, uint32_t*, uint32_t*,
+                              const uint32_t*, uint32_t*, const uint8_t*, uint32_t*, uint32_t*, uint32_t*, uint32_t*,
                               const uint32_t*, uint32_t, int*);
+
+// Hours 2..6 of a day change nothing once hour 1 has sent everyone but hospital staff home
+// (routine, citizen/mod.rs:243-247, sets current_area = home_location and nothing else), so
+// when the previous hour ran in the same segment the hour's kernel is skipped and its
+// counts row repeats the previous one.
+static bool sleep_hour_skipped(uint32_t first_hour, uint32_t k) {
+    const uint32_t hod = (first_hour + k) % 24u;
+    return k > 0 && hod >= 2u && hod <= 6u;
+}
 
 // The k_decide instance of an hour of the day.
 static DecideKernel decide_kernel(uint32_t hod) {
@@ -254,6 +300,7 @@ static int enqueue_hours(epi_engine* h, uint32_t first_hour, uint32_t nh) {
         const uint32_t hod = (first_hour + k) % 24u;
         uint32_t* rows = h->d_counts + (size_t)k * row_words;
         if (k > 0 && (first_hour + k) % kClaimWindow == 0) CK(cudaMemsetAsync(h->d_claim, 0xFF, h->claim_cells * sizeof(uint32_t), h->stream));
+        if (sleep_hour_skipped(first_hour, k)) continue;
         if (hod >= 1u && hod <= 6u) {
             LAUNCH(kKSleep, (k_sleep<<<h->grid_blocks, kThreads, 0, h->stream>>>(h->d_params, h->d_chunk_rep, n_chunks,
                                                                                   h->d_st, rows)));
@@ -261,10 +308,11 @@ static int enqueue_hours(epi_engine* h, uint32_t first_hour, uint32_t nh) {
             const DecideKernel decide = decide_kernel(hod);
             LAUNCH(kKDecide, (decide<<<h->grid_blocks, kThreads, 0, h->stream>>>(
                                   h->d_params, h->d_chunk_rep, n_chunks, h->d_pos, h->d_st, h->d_home, h->d_work, h->d_wsa,
-                                  h->d_plane, h->d_claim, h->d_tgt, rows, h->d_hour_base, k, h->d_err)));
+                                  h->d_plane, h->d_claim, h->d_tgt, h->d_lost, rows, h->d_hour_base, k, h->d_err)));
             LAUNCH(kKCommit, (k_commit<<<h->commit_blocks, kThreads, 0, h->stream>>>(h->d_params, h->d_chunk_rep, h->slots,
                                                                                      h->d_pos, h->d_tgt, h->d_plane,
-                                                                                     h->d_claim, h->d_hour_base, k)));
+                                                                                     h->d_claim, h->d_lost, h->d_hour_base,
+                                                                                     k)));
         }
     }
     CK(cudaMemcpyAsync(h->h_counts, h->d_counts, (size_t)nh * row_words * sizeof(uint32_t), cudaMemcpyDeviceToHost,
@@ -294,34 +342,46 @@ static int run_hours(epi_engine* h, uint32_t first_hour, uint32_t nh) {
     if (h->last_claim_hour >= 0 &&
         ((int64_t)first_hour <= h->last_claim_hour || first_hour / kClaimWindow != (uint64_t)h->last_claim_hour / kClaimWindow))
         CK(cudaMemsetAsync(h->d_claim, 0xFF, h->claim_cells * sizeof(uint32_t), h->stream));
+    if (h->last_claim_hour >= (int64_t)first_hour)  // loss marks of hours about to run again
+        CK(cudaMemsetAsync(h->d_lost, 0xFF, (size_t)h->slots * sizeof(uint32_t), h->stream));
     h->last_claim_hour = (int64_t)first_hour + nh - 1;
     *h->h_hour_base = first_hour;
     CK(cudaMemcpyAsync(h->d_hour_base, h->h_hour_base, sizeof(uint32_t), cudaMemcpyHostToDevice, h->stream));
-    if (h->profiling) {
-        rc = enqueue_hours(h, first_hour, nh);
-        if (rc) return rc;
-    } else {
+    {
         // the kernel sequence depends on the hours of the day and on where a claim window opens
-        auto key = std::make_pair(first_hour % 24u + 24u * window_start_offset(first_hour, nh), nh);
+        auto key = std::make_tuple(first_hour % 24u + 24u * window_start_offset(first_hour, nh), nh, h->profiling);
         auto it = h->graphs.find(key);
         if (it == h->graphs.end()) {
+            epi_engine::HourGraph hg;
             cudaGraph_t g;
             CK(cudaStreamBeginCapture(h->stream, cudaStreamCaptureModeThreadLocal));
+            h->capture = &hg.events;
             rc = enqueue_hours(h, first_hour, nh);
+            h->capture = nullptr;
             cudaError_t ce = cudaStreamEndCapture(h->stream, &g);
-            if (rc) return rc;
-            if (ce != cudaSuccess) { h->err = std::string("graph capture: ") + cudaGetErrorString(ce); return EPI_ERR_CUDA; }
-            cudaGraphExec_t ge;
-            ce = cudaGraphInstantiate(&ge, g, 0);
-            cudaGraphDestroy(g);
-            if (ce != cudaSuccess) { h->err = std::string("graph instantiate: ") + cudaGetErrorString(ce); return EPI_ERR_CUDA; }
-            it = h->graphs.emplace(key, ge).first;
+            if (rc == EPI_OK && ce == cudaSuccess) {
+                ce = cudaGraphInstantiate(&hg.exec, g, 0);
+                cudaGraphDestroy(g);
+            }
+            if (rc != EPI_OK || ce != cudaSuccess) {
+                for (auto& t : hg.events) { cudaEventDestroy(t.begin); cudaEventDestroy(t.end); }
+                if (rc) return rc;
+                h->err = std::string("hour graph: ") + cudaGetErrorString(ce);
+                return EPI_ERR_CUDA;
+            }
+            it = h->graphs.emplace(key, std::move(hg)).first;
         }
-        CK(cudaGraphLaunch(it->second, h->stream));
+        CK(cudaGraphLaunch(it->second.exec, h->stream));
+        h->pending.insert(h->pending.end(), it->second.events.begin(), it->second.events.end());
     }
     CK(cudaStreamSynchronize(h->stream));
     for (uint32_t k = 0; k < nh; ++k) {
         const uint32_t hod = (first_hour + k) % 24u;
+        if (sleep_hour_skipped(first_hour, k)) {
+            std::memcpy(h->h_counts + (size_t)k * h->R() * 8, h->h_counts + (size_t)(k - 1) * h->R() * 8,
+                        (size_t)h->R() * 8 * sizeof(uint32_t));
+            continue;
+        }
         h->kernels_launched += (hod >= 1u && hod <= 6u) ? 1u : 2u;
     }
     rc = harvest_events(h);
@@ -482,15 +542,15 @@ static int run_loop_body(epi_engine* h) {
 
 // ------------------------------------------------------------------ create / destroy
 static void free_device(epi_engine* h) {
-    for (auto& g : h->graphs) cudaGraphExecDestroy(g.second);
-    h->graphs.clear();
+    destroy_graphs(h);
     cudaFree(h->d_params); cudaFree(h->d_chunk_rep); cudaFree(h->d_pos); cudaFree(h->d_home); cudaFree(h->d_work);
-    cudaFree(h->d_wsa); cudaFree(h->d_tgt); cudaFree(h->d_st); cudaFree(h->d_plane); cudaFree(h->d_claim);
+    cudaFree(h->d_wsa); cudaFree(h->d_tgt); cudaFree(h->d_lost); cudaFree(h->d_st); cudaFree(h->d_plane); cudaFree(h->d_claim);
     cudaFree(h->d_counts); cudaFree(h->d_hour_base); cudaFree(h->d_err); cudaFree(h->d_scratch);
     cudaFree(h->s_pos); cudaFree(h->s_wsa); cudaFree(h->s_st); cudaFree(h->s_plane);
     if (h->h_counts) cudaFreeHost(h->h_counts);
     if (h->h_hour_base) cudaFreeHost(h->h_hour_base);
-    for (auto& pe : h->pending) { cudaEventDestroy(pe.second.first); cudaEventDestroy(pe.second.second); }
+    for (auto& pe : h->pending)
+        if (pe.pooled) { cudaEventDestroy(pe.begin); cudaEventDestroy(pe.end); }
     for (auto e : h->event_pool) cudaEventDestroy(e);
     if (h->own_stream && h->stream) cudaStreamDestroy(h->stream);
 }
@@ -595,6 +655,7 @@ static int engine_init(epi_engine* h, const epi_params* params, const epi_agent_
     CK(cudaMalloc(&h->d_work, slots * sizeof(uint32_t)));
     CK(cudaMalloc(&h->d_wsa, slots * sizeof(uint32_t)));
     CK(cudaMalloc(&h->d_tgt, slots * sizeof(uint32_t)));
+    CK(cudaMalloc(&h->d_lost, slots * sizeof(uint32_t)));
     CK(cudaMalloc(&h->d_st, slots * sizeof(uint2)));
     CK(cudaMalloc(&h->d_plane, h->plane_bytes));
     CK(cudaMalloc(&h->d_claim, h->claim_cells * sizeof(uint32_t)));
@@ -625,6 +686,7 @@ static int engine_init(epi_engine* h, const epi_params* params, const epi_agent_
     CK(cudaMemcpyAsync(h->d_wsa, wsa.data(), slots * sizeof(uint32_t), cudaMemcpyHostToDevice, h->stream));
     CK(cudaMemcpyAsync(h->d_st, st.data(), slots * sizeof(uint2), cudaMemcpyHostToDevice, h->stream));
     CK(cudaMemsetAsync(h->d_tgt, 0xFF, slots * sizeof(uint32_t), h->stream));
+    CK(cudaMemsetAsync(h->d_lost, 0xFF, slots * sizeof(uint32_t), h->stream));
     CK(cudaMemsetAsync(h->d_plane, 0, h->plane_bytes, h->stream));
     CK(cudaMemsetAsync(h->d_claim, 0xFF, h->claim_cells * sizeof(uint32_t), h->stream));
     CK(cudaMemsetAsync(h->d_err, 0, sizeof(int), h->stream));
@@ -754,6 +816,7 @@ static int restore_state(epi_engine* h) {
     CK(cudaMemcpyAsync(h->d_st, h->s_st, n * sizeof(uint2), cudaMemcpyDeviceToDevice, h->stream));
     CK(cudaMemcpyAsync(h->d_plane, h->s_plane, h->plane_bytes, cudaMemcpyDeviceToDevice, h->stream));
     CK(cudaMemsetAsync(h->d_tgt, 0xFF, n * sizeof(uint32_t), h->stream));
+    CK(cudaMemsetAsync(h->d_lost, 0xFF, n * sizeof(uint32_t), h->stream));
     CK(cudaMemsetAsync(h->d_claim, 0xFF, h->claim_cells * sizeof(uint32_t), h->stream));
     h->last_claim_hour = -1;
     for (auto& rep : h->reps) {
@@ -1216,8 +1279,9 @@ extern "C" int epi_tick_hour_noalloc(const epi_params* params, uint32_t hour, ui
         NOALLOC_CK(cudaMemsetAsync(d_claim, 0xFF, claim_bytes, s));
         const DecideKernel decide = decide_kernel(hod);
         decide<<<blocks, kThreads, 0, s>>>(d_params, nullptr, n_chunks, pos, st, home, work, work_start_at, plane, d_claim,
-                                           d_tgt, counts, d_hour, 0u, d_err);
-        k_commit<<<commit_blocks_for(n), kThreads, 0, s>>>(d_params, nullptr, n, pos, d_tgt, plane, d_claim, d_hour, 0u);
+                                           d_tgt, nullptr, counts, d_hour, 0u, d_err);
+        k_commit<<<commit_blocks_for(n), kThreads, 0, s>>>(d_params, nullptr, n, pos, d_tgt, plane, d_claim, nullptr,
+                                                           d_hour, 0u);
     }
     NOALLOC_CK(cudaGetLastError());
     int err = 0;

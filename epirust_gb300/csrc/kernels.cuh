@@ -114,9 +114,9 @@ __global__ void __launch_bounds__(kThreads) k_decide(const DevParams* __restrict
                                                      uint2* __restrict__ st, const uint32_t* __restrict__ home,
                                                      const uint32_t* __restrict__ work, uint32_t* __restrict__ wsa,
                                                      const uint8_t* __restrict__ plane, uint32_t* __restrict__ claim,
-                                                     uint32_t* __restrict__ tgt, uint32_t* __restrict__ counts,
-                                                     const uint32_t* __restrict__ hour_base, uint32_t hour_offset,
-                                                     int* err) {
+                                                     uint32_t* __restrict__ tgt, uint32_t* __restrict__ lost,
+                                                     uint32_t* __restrict__ counts, const uint32_t* __restrict__ hour_base,
+                                                     uint32_t hour_offset, int* err) {
     __shared__ uint32_t sh[8];
     __shared__ DevParams sP;
     const DevParams& P = sP;
@@ -158,6 +158,7 @@ __global__ void __launch_bounds__(kThreads) k_decide(const DevParams* __restrict
             const Cell cell{unpack_x(p), unpack_y(p)};
             Draws dr{i, hour, P.key0, P.key1};
             Cell nc;
+            bool infect = false;
             if (HC == kHcStart) {
                 nc = routine_start(P, pl, s, hm, cell, hosp_first, dr);
             } else if (HC == kHcEnd) {
@@ -165,7 +166,7 @@ __global__ void __launch_bounds__(kThreads) k_decide(const DevParams* __restrict
             } else {
                 const bool staff = st_ws(s) == EPI_WS_HOSPITAL_STAFF;
                 uint32_t w0 = staff ? wsa[slot] : 0u, w = w0;
-                nc = perform_movements<HC>(P, pl, s, at, w, hm, wk, cell, hod, hour, dr);
+                nc = perform_movements<HC>(P, pl, s, w, hm, wk, cell, hod, hour, dr, infect);
                 if (staff && w != w0) wsa[slot] = w;
             }
             bool moving = nc.x != cell.x || nc.y != cell.y;
@@ -174,8 +175,26 @@ __global__ void __launch_bounds__(kThreads) k_decide(const DevParams* __restrict
                 moving = false;
                 nc = cell;
             }
+            // The claim goes out before the infection update so that its round trip overlaps it.
+            const uint32_t key = claim_key(hour, i);
+            const uint32_t old = moving ? atomicMin(&rclaim[(size_t)nc.y * P.W + nc.x], key) : kNoClaim;
+            if (infect) infection_dynamics(P, pl, s, at, area_rect(P, st_area(s), hm, wk), nc, hour, dr);
             const uint32_t cls = cell_class(P, s);
-            if (moving) atomicMin(&rclaim[(size_t)nc.y * P.W + nc.x], claim_key(hour, i));
+            if (moving) {
+                // The claim that atomicMin finds names an agent this one competes with: of
+                // the two the higher index loses.  Every claimant but the cell's lowest is
+                // named so, by itself or by the claimant that displaced it, so the loss
+                // marks settle the cell without a second read of the claim plane.
+                if (lost && old != kNoClaim && (old >> kClaimAgentBits) == (key >> kClaimAgentBits)) {
+                    const uint32_t j = old & kMaxAgentsPerWorld;
+                    if (j < i) {
+                        moving = false;
+                        nc = cell;
+                    } else {
+                        lost[P.agent_off + j] = hour;
+                    }
+                }
+            }
             tgt[slot] = (moving || cls != cell_class(P, s0)) ? encode_target(nc, cls) : kNoAction;
             if (s != s0 || at != at0) st[slot] = make_uint2(s, at);
             bin = count_bin(s);
@@ -187,23 +206,26 @@ __global__ void __launch_bounds__(kThreads) k_decide(const DevParams* __restrict
 
 // Resolve the claims of the hour: the lowest index that claimed a cell moves there
 // (the serial resolve of allocation_map.rs:93-102 in index order), others keep their cell.
-// Each thread takes kCommitSlots slots a block-width apart, issuing all their independent
-// loads before the dependent claim reads.
+// With loss marks (lost != nullptr) a mover wins unless k_decide marked it beaten this
+// hour; without them the winner is read from the claim plane.  Each thread takes
+// kCommitSlots slots a block-width apart, issuing all their independent loads first.
 constexpr int kCommitSlots = 4;
 
 __global__ void __launch_bounds__(kThreads) k_commit(const DevParams* __restrict__ Pall, const uint32_t* __restrict__ chunk_rep,
                                                      uint32_t n_slots, uint32_t* __restrict__ pos,
                                                      const uint32_t* __restrict__ tgt, uint8_t* __restrict__ plane,
                                                      const uint32_t* __restrict__ claim,
+                                                     const uint32_t* __restrict__ lost,
                                                      const uint32_t* __restrict__ hour_base, uint32_t hour_offset) {
     const uint32_t hour = *hour_base + hour_offset;
     const uint32_t base = blockIdx.x * (blockDim.x * kCommitSlots) + threadIdx.x;
-    uint32_t t[kCommitSlots], p[kCommitSlots];
+    uint32_t t[kCommitSlots], p[kCommitSlots], l[kCommitSlots];
 #pragma unroll
     for (int k = 0; k < kCommitSlots; ++k) {
         const uint32_t slot = base + k * blockDim.x;
         t[k] = slot < n_slots ? tgt[slot] : kNoAction;
         p[k] = slot < n_slots ? pos[slot] : 0u;
+        l[k] = lost && slot < n_slots ? lost[slot] : 0u;
     }
     const DevParams* Pr[kCommitSlots];
     uint32_t won[kCommitSlots];
@@ -211,10 +233,11 @@ __global__ void __launch_bounds__(kThreads) k_commit(const DevParams* __restrict
     for (int k = 0; k < kCommitSlots; ++k) {
         const uint32_t slot = base + k * blockDim.x;
         Pr[k] = Pall + (chunk_rep && t[k] != kNoAction ? chunk_rep[slot / kChunk] : 0u);
-        won[k] = kNoClaim;  // no claim read: never equal to a key
+        won[k] = kNoClaim;  // never equal to a key: stays put
         if (t[k] != kNoAction && target_xy(t[k]) != p[k]) {
             const uint32_t xy = target_xy(t[k]);
-            won[k] = claim[Pr[k]->claim_off + (size_t)unpack_y(xy) * (uint32_t)Pr[k]->W + unpack_x(xy)];
+            if (lost) won[k] = l[k] == hour ? kNoClaim : claim_key(hour, slot - Pr[k]->agent_off);
+            else won[k] = claim[Pr[k]->claim_off + (size_t)unpack_y(xy) * (uint32_t)Pr[k]->W + unpack_x(xy)];
         }
     }
 #pragma unroll

@@ -290,16 +290,18 @@ __device__ __forceinline__ bool staff_movements(const DevParams& P, const PlaneV
 }
 
 // Citizen::perform_movements, citizen/mod.rs:257-349, for the movement classes (hours 7..22):
-// the work-status arms (Normal|Essential, HospitalStaff, NA) at hour class HC, then the
-// infection update of DiseaseStateMachine::next.
+// the work-status arms (Normal|Essential, HospitalStaff, NA) at hour class HC.  Returns the
+// proposed cell; infect is cleared when the hour ends before the infection update of
+// DiseaseStateMachine::next, which the caller runs on the proposed cell otherwise.
 template <int HC>
-__device__ __forceinline__ Cell perform_movements(const DevParams& P, const PlaneView& pl, uint32_t& s, uint32_t& at,
-                                                  uint32_t& wsa, uint32_t home, uint32_t work, Cell cell,
-                                                  uint32_t hod, uint32_t hour, Draws& dr) {
+__device__ __forceinline__ Cell perform_movements(const DevParams& P, const PlaneView& pl, uint32_t& s, uint32_t& wsa,
+                                                  uint32_t home, uint32_t work, Cell cell, uint32_t hod, uint32_t hour,
+                                                  Draws& dr, bool& infect) {
     const uint32_t ws = st_ws(s);
     Cell nc = cell;
+    infect = true;
     if (ws == EPI_WS_HOSPITAL_STAFF) {
-        if (!staff_movements(P, pl, s, wsa, home, work, cell, nc, hod, hour, dr)) return nc;
+        infect = staff_movements(P, pl, s, wsa, home, work, cell, nc, hod, hour, dr);
     } else {
         const Rect cur = area_rect(P, st_area(s), home, work);
         const bool worker = ws != EPI_WS_NA;  // Normal or Essential here
@@ -336,7 +338,6 @@ __device__ __forceinline__ Cell perform_movements(const DevParams& P, const Plan
             }
         }
     }
-    infection_dynamics(P, pl, s, at, area_rect(P, st_area(s), home, work), nc, hour, dr);
     return nc;
 }
 
