@@ -107,6 +107,21 @@ EXPORTS = [
     "epi_ensemble_kernels_launched", "epi_ensemble_hour_bytes",
 ]
 
+# include/epi_surrogate.h
+MLP_EXPORTS = [
+    "epi_mlp_create", "epi_mlp_destroy", "epi_mlp_last_error", "epi_mlp_set_stream", "epi_mlp_param_count",
+    "epi_mlp_get_params", "epi_mlp_set_params", "epi_mlp_set_dataset", "epi_mlp_train", "epi_mlp_gradients",
+    "epi_mlp_predict", "epi_mlp_score", "epi_mlp_kernels_launched",
+]
+
+
+class MlpConfig(C.Structure):
+    _fields_ = [
+        ("in_dim", C.c_uint32), ("hidden", C.c_uint32), ("hidden_layers", C.c_uint32), ("out_dim", C.c_uint32),
+        ("batch", C.c_uint32), ("lr", C.c_float), ("beta1", C.c_float), ("beta2", C.c_float), ("eps", C.c_float),
+        ("seed", C.c_uint64),
+    ]
+
 _lib = None
 
 
@@ -181,6 +196,20 @@ def lib():
     _sig(L, "epi_ensemble_kernels_launched", C.c_int, [V, P(C.c_uint64)])
     _sig(L, "epi_ensemble_hour_bytes", C.c_int, [V, C.c_uint32, P(C.c_double)])
     _sig(L, "epi_tick_hour_noalloc", C.c_int, [P(EpiParams), C.c_uint32, C.c_uint32, V, V, V, V, V, V, V, V])
+    F = P(C.c_float)
+    _sig(L, "epi_mlp_create", C.c_int, [P(MlpConfig), P(V)])
+    _sig(L, "epi_mlp_destroy", C.c_int, [V])
+    _sig(L, "epi_mlp_last_error", C.c_char_p, [V])
+    _sig(L, "epi_mlp_set_stream", C.c_int, [V, V])
+    _sig(L, "epi_mlp_param_count", C.c_int, [V, P(C.c_uint64)])
+    _sig(L, "epi_mlp_get_params", C.c_int, [V, F])
+    _sig(L, "epi_mlp_set_params", C.c_int, [V, F])
+    _sig(L, "epi_mlp_set_dataset", C.c_int, [V, F, F, C.c_uint32])
+    _sig(L, "epi_mlp_train", C.c_int, [V, C.c_uint32, C.c_uint64, F])
+    _sig(L, "epi_mlp_gradients", C.c_int, [V, F, F, C.c_uint32, F, F])
+    _sig(L, "epi_mlp_predict", C.c_int, [V, F, C.c_uint32, F])
+    _sig(L, "epi_mlp_score", C.c_int, [V, F, C.c_uint32, F, F])
+    _sig(L, "epi_mlp_kernels_launched", C.c_int, [V, P(C.c_uint64)])
     _lib = L
     return L
 

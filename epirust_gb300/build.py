@@ -24,7 +24,7 @@ NVCC_FLAGS = ARCH + ["-O3", "-lineinfo", "-std=c++17", "-Xcompiler", "-fPIC,-ffp
                      "-Xptxas", "-warn-spills"]
 CXX_FLAGS = ["-O2", "-std=c++17", "-fPIC", "-ffp-contract=off", "-Wall", "-Wextra", "-Wno-unused-parameter"]
 
-CU_SOURCES = ["engine.cu"]
+CU_SOURCES = ["engine.cu", "surrogate.cu"]
 CXX_SOURCES = ["host.cpp"]
 
 
@@ -55,7 +55,7 @@ def build(verbose: bool = False) -> str:
     os.makedirs(OUT, exist_ok=True)
     nvcc = _nvcc()
     headers = [os.path.join(CSRC, f) for f in os.listdir(CSRC) if f.endswith((".h", ".hpp", ".cuh"))]
-    headers.append(os.path.join(HERE, "..", "include", "epi_engine.h"))
+    headers += [os.path.join(HERE, "..", "include", f) for f in ("epi_engine.h", "epi_surrogate.h")]
     jobs = []
     objs = []
     for src in CU_SOURCES:

@@ -20,6 +20,7 @@
 #include <utility>
 #include <vector>
 
+#include "../../include/epi_surrogate.h"
 #include "host.hpp"
 #include "kernels.cuh"
 
@@ -1065,6 +1066,7 @@ size_t epi_abi_struct_size(const char* name) {
     if (!std::strcmp(name, "epi_agent_record")) return sizeof(epi_agent_record);
     if (!std::strcmp(name, "epi_counts")) return sizeof(epi_counts);
     if (!std::strcmp(name, "epi_geography")) return sizeof(epi_geography);
+    if (!std::strcmp(name, "epi_mlp_config")) return sizeof(epi_mlp_config);
     return 0;
 }
 

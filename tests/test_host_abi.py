@@ -15,21 +15,22 @@ from helpers import COVID_FAST, SMALL_POX, diff_records, golden, make_config
 ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
 
 
-def _declared_functions():
-    text = open(os.path.join(ROOT, "include", "epi_engine.h")).read()
+def _declared_functions(header="epi_engine.h"):
+    text = open(os.path.join(ROOT, "include", header)).read()
     text = re.sub(r"/\*.*?\*/", "", text, flags=re.S)
     return sorted(set(re.findall(r"\b(epi_[a-z_]+)\s*\(", text)))
 
 
-def test_library_exports_every_declared_symbol(engine_built):
+@pytest.mark.parametrize("header,exports", [("epi_engine.h", "EXPORTS"), ("epi_surrogate.h", "MLP_EXPORTS")])
+def test_library_exports_every_declared_symbol(engine_built, header, exports):
     from epirust_gb300 import _lib
 
     L = C.CDLL(engine_built)
-    declared = _declared_functions()
-    assert len(declared) >= 30
+    declared = _declared_functions(header)
+    assert len(declared) >= 10
     missing = [f for f in declared if not hasattr(L, f)]
     assert not missing, f"missing exports: {missing}"
-    assert sorted(_lib.EXPORTS) == declared
+    assert sorted(getattr(_lib, exports)) == declared
     nm = subprocess.run(["nm", "-D", "--defined-only", engine_built], capture_output=True, text=True).stdout
     for f in declared:
         assert re.search(rf"\bT {f}$", nm, flags=re.M), f
@@ -43,6 +44,7 @@ def test_struct_layouts_match(engine_built):
     assert L.epi_abi_struct_size(b"epi_agent_record") == _lib.AGENT_DTYPE.itemsize == 56
     assert L.epi_abi_struct_size(b"epi_counts") == C.sizeof(_lib.EpiCounts) == 28
     assert L.epi_abi_struct_size(b"epi_geography") == C.sizeof(_lib.EpiGeography)
+    assert L.epi_abi_struct_size(b"epi_mlp_config") == C.sizeof(_lib.MlpConfig) == 48
     assert L.epi_abi_struct_size(b"nope") == 0
 
 
