@@ -74,17 +74,23 @@ def uniform_candidates(n: int, dims: int, seed: int) -> np.ndarray:
     return np.random.default_rng(seed).random((n, dims))
 
 
-def config_for(p: dict, agents: int, grid: int, hours: int, seed: int) -> dict:
+def config_for(p: dict, agents: int, grid: int, hours: int, seed: int, per_agents: int | None = None) -> dict:
+    """Engine config of one parameter point.  The two head counts (initial infections and the
+    lockdown threshold) are per `per_agents` agents and scale with the population, so that
+    normalised curves of worlds of different sizes are comparable; per_agents=None keeps them
+    as absolute counts."""
+    scale = 1.0 if per_agents is None else agents / per_agents
     disease = dict(SMALL_POX)
     disease["regular_transmission_rate"] = p["regular_transmission_rate"]
     disease["high_transmission_rate"] = p["high_transmission_rate"]
     disease["death_rate"] = p["death_rate"]
     interventions = [
-        {"Lockdown": {"at_number_of_infections": int(p["lockdown_at_number_of_infections"]),
+        {"Lockdown": {"at_number_of_infections": max(1, int(round(p["lockdown_at_number_of_infections"] * scale))),
                       "essential_workers_population": p["essential_workers_population"]}},
         {"Vaccinate": {"at_hour": int(p["vaccination_hour"]), "percent": p["vaccination_percent"]}},
     ]
-    return config_dict(agents, grid, hours, seed, disease, exposed=int(p["initial_infected"]), interventions=interventions)
+    exposed = max(1, int(round(p["initial_infected"] * scale)))
+    return config_dict(agents, grid, hours, seed, disease, exposed=exposed, interventions=interventions)
 
 
 def curves_from_rows(rows: np.ndarray, n: int, days: int) -> np.ndarray:
@@ -115,6 +121,16 @@ def simulate_curves(configs: list[dict], days: int, batch: int = 512) -> np.ndar
             n = c["population"]["Auto"]["number_of_agents"]
             out[s + i] = curves_from_rows(r, n, days).ravel()
     return out
+
+
+def compartment_scaling(y: np.ndarray, days: int, floor: float = 1e-6):
+    """Output standardisation of (n, 6 * days) curves: the mean of every output and one scale
+    per compartment (its standard deviation over samples and days), so that the small
+    compartments weigh as much in the loss as the large ones."""
+    y = np.asarray(y, dtype=np.float64)
+    mean = y.mean(axis=0)
+    sd = (y - mean).reshape(len(y), 6, days).std(axis=(0, 2))
+    return mean, np.repeat(np.maximum(sd, floor), days)
 
 
 def peak_height(curves: np.ndarray, days: int) -> np.ndarray:
@@ -175,8 +191,26 @@ class Surrogate:
         assert a.size == self.n_params
         self._check(lib().epi_mlp_set_params(self._h, self._ptr(a)))
 
+    def set_output_scaling(self, mean, scale) -> None:
+        """Train and predict in standardised outputs z = (y - mean) / scale (host side);
+        predict() and score() take and return y."""
+        self.y_mean = np.asarray(mean, dtype=np.float64).ravel()
+        self.y_scale = np.asarray(scale, dtype=np.float64).ravel()
+        assert self.y_mean.size == self.cfg.out_dim and self.y_scale.size == self.cfg.out_dim
+        assert (self.y_scale > 0).all()
+
+    def _to_z(self, y) -> np.ndarray:
+        if getattr(self, "y_mean", None) is None:
+            return self._f32(y)
+        return self._f32((np.asarray(y, dtype=np.float64) - self.y_mean) / self.y_scale)
+
+    def _from_z(self, z) -> np.ndarray:
+        if getattr(self, "y_mean", None) is None:
+            return z
+        return (z * self.y_scale + self.y_mean).astype(np.float32)
+
     def set_dataset(self, x, y) -> None:
-        x, y = self._f32(x), self._f32(y)
+        x, y = self._f32(x), self._to_z(y)
         assert x.shape[0] == y.shape[0] and x.shape[1] == self.cfg.in_dim and y.shape[1] == self.cfg.out_dim
         self._check(lib().epi_mlp_set_dataset(self._h, self._ptr(x), self._ptr(y), x.shape[0]))
 
@@ -197,10 +231,12 @@ class Surrogate:
         x = self._f32(x)
         y = np.zeros((x.shape[0], self.cfg.out_dim), dtype=np.float32)
         self._check(lib().epi_mlp_predict(self._h, self._ptr(x), x.shape[0], self._ptr(y)))
-        return y
+        return self._from_z(y)
 
     def score(self, x, target) -> np.ndarray:
-        x, t = self._f32(x), self._f32(target)
+        """Squared distance to the target, summed over outputs, in the training scale (the
+        standardised outputs when set_output_scaling was called)."""
+        x, t = self._f32(x), self._to_z(np.asarray(target)[None])[0]
         s = np.zeros(x.shape[0], dtype=np.float32)
         self._check(lib().epi_mlp_score(self._h, self._ptr(x), x.shape[0], self._ptr(t), self._ptr(s)))
         return s

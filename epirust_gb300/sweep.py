@@ -1,0 +1,142 @@
+"""Surrogate training on GPU-ABM ensembles and the surrogate-screened parameter sweep.
+
+train_on_abm():  Latin-hypercube parameter points -> batched GPU-ABM runs -> daily S/E/I/H/R/D
+                 curves (normalised) -> an ensemble of MLPs trained with Adam on the tensor
+                 cores; held-out error against the ABM and against the training-mean curve.
+screened_sweep(): a target curve from hidden parameters (ABM at full size), candidates scored
+                 by the surrogate ensemble, the best re-run by the batched ABM with several
+                 replicates each, and the same ABM budget spent on unscreened candidates.
+
+Times are wall-clock around calls that return after the device has finished (the ABM
+through epi_ensemble_run, the network through epi_mlp_*).
+"""
+from __future__ import annotations
+
+import math
+import time
+
+import numpy as np
+
+from .surrogate import (PARAMS, Surrogate, compartment_scaling, config_for, denormalise, latin_hypercube,
+                        relative_peak_error, screen, simulate_curves, uniform_candidates, unit_distance)
+
+
+def _flops(in_dim: int, hidden: int, layers: int, out_dim: int) -> float:
+    """Multiply-adds x 2 of one forward pass (unpadded shapes)."""
+    dims = [in_dim] + [hidden] * layers + [out_dim]
+    return 2.0 * sum(dims[i] * dims[i + 1] for i in range(len(dims) - 1))
+
+
+def grid_for(agents: int, density: float = 0.16) -> int:
+    return int(math.ceil(math.sqrt(agents / density)))
+
+
+def train_on_abm(runs: int = 4096, held_out: int = 512, agents: int = 100_000, days: int = 100,
+                 members: int = 5, steps: int = 3000, seed: int = 4, hidden: int = 512, hidden_layers: int = 3,
+                 batch: int = 256, abm_batch: int = 512, per_agents: int = 100_000, curves: np.ndarray | None = None):
+    """curves: ABM curves of this design computed before (skips the ABM stage)."""
+    grid = grid_for(agents)
+    hours = 24 * days + 1
+    u = latin_hypercube(runs, len(PARAMS), seed)
+    cfgs = [config_for(d, agents, grid, hours, seed=seed * 1_000_003 + i, per_agents=per_agents)
+            for i, d in enumerate(denormalise(u))]
+    t0 = time.perf_counter()
+    y = simulate_curves(cfgs, days, batch=abm_batch) if curves is None else np.asarray(curves, dtype=np.float32)
+    t_abm = time.perf_counter() - t0
+    n_tr = runs - held_out
+    xtr, ytr, xte, yte = u[:n_tr], y[:n_tr], u[n_tr:], y[n_tr:]
+    nets, losses = [], []
+    mean, scale = compartment_scaling(ytr, days)
+    t0 = time.perf_counter()
+    for m in range(members):
+        net = Surrogate(in_dim=len(PARAMS), out_dim=6 * days, hidden=hidden, hidden_layers=hidden_layers,
+                        batch=batch, seed=seed * 101 + m)
+        net.set_output_scaling(mean, scale)
+        net.set_dataset(xtr, ytr)
+        losses.append(net.train(steps, seed=seed * 7 + m))
+        nets.append(net)
+    t_train = time.perf_counter() - t0
+    preds = np.stack([n.predict(xte) for n in nets])
+    mean_pred = preds.mean(axis=0)
+    mse_net = float(np.mean((mean_pred - yte) ** 2))
+    mse_mean = float(np.mean((ytr.mean(axis=0) - yte) ** 2))
+    pe = relative_peak_error(mean_pred, yte, days)
+    samples = members * steps * batch
+    flop = 3.0 * _flops(len(PARAMS), hidden, hidden_layers, 6 * days) * samples  # forward + backward ~ 3x forward
+    info = {
+        "runs": runs, "held_out": held_out, "agents": agents, "grid": grid, "days": days,
+        "abm_s": t_abm, "abm_agent_hours_per_s": runs * agents * (hours - 1) / t_abm,
+        "members": members, "steps": steps, "batch": batch, "train_s": t_train,
+        "train_samples_per_s": samples / t_train, "train_tflops": flop / t_train / 1e12,
+        "final_loss": [float(l[-20:].mean()) for l in losses],
+        "held_out_mse": mse_net, "mean_curve_mse": mse_mean, "gain_vs_mean_curve": mse_mean / max(mse_net, 1e-30),
+        "held_out_peak_rel_err_median": float(np.median(pe)), "held_out_peak_rel_err_p90": float(np.quantile(pe, 0.9)),
+    }
+    info["curves"] = y
+    return nets, info
+
+
+def screened_sweep(nets, candidates: int = 65_536, keep: int = 256, replicates: int = 8, agents: int = 1_000_000,
+                   days: int = 100, seed: int = 99, peak_tolerance: float = 0.05, abm_batch: int = 64,
+                   per_agents: int = 100_000):
+    grid = grid_for(agents)
+    hours = 24 * days + 1
+    rng = np.random.default_rng(seed)
+    hidden = rng.random((1, len(PARAMS)))
+    t0 = time.perf_counter()
+    target = simulate_curves([config_for(denormalise(hidden)[0], agents, grid, hours, seed=seed, per_agents=per_agents)],
+                             days)[0]
+    t_target = time.perf_counter() - t0
+    cand = uniform_candidates(candidates, len(PARAMS), seed + 1)
+
+    # surrogate screen
+    t0 = time.perf_counter()
+    best, best_scores, flagged = screen(nets, cand, target, keep, days, peak_tolerance)
+    t_screen = time.perf_counter() - t0
+    member_preds = np.stack([n.predict(cand[best]) for n in nets])
+
+    def abm(points: np.ndarray, base_seed: int) -> np.ndarray:
+        cfgs = [config_for(d, agents, grid, hours, seed=base_seed + 97 * i + r, per_agents=per_agents)
+                for i, d in enumerate(denormalise(points)) for r in range(replicates)]
+        return simulate_curves(cfgs, days, batch=abm_batch).reshape(len(points), replicates, -1)
+
+    t0 = time.perf_counter()
+    runs_s = abm(cand[best], 10_000)
+    t_abm_screened = time.perf_counter() - t0
+    mean_s = runs_s.mean(axis=1)
+    err_s = ((mean_s - target) ** 2).mean(axis=1)
+    pick = int(np.argmin(err_s))
+
+    # the same ABM budget on unscreened candidates
+    rand_idx = np.random.default_rng(seed + 2).choice(candidates, keep, replace=False)
+    t0 = time.perf_counter()
+    runs_r = abm(cand[rand_idx], 20_000)
+    t_abm_random = time.perf_counter() - t0
+    mean_r = runs_r.mean(axis=1)
+    err_r = ((mean_r - target) ** 2).mean(axis=1)
+    pick_r = int(np.argmin(err_r))
+
+    # surrogate vs ABM ensemble mean at the screened candidates (the stated error criterion)
+    sur_mean = member_preds.mean(axis=0)
+    peak_err = relative_peak_error(sur_mean, mean_s, days)
+    per_run_s = t_abm_screened / (keep * replicates)
+    abm_only_s = candidates * replicates * per_run_s  # every candidate through the ABM at the measured rate
+    screened_s = t_screen + t_abm_screened
+    return {
+        "candidates": candidates, "keep": keep, "replicates": replicates, "agents": agents, "grid": grid,
+        "days": days, "target_abm_s": t_target, "screen_s": t_screen, "abm_screened_s": t_abm_screened,
+        "abm_random_s": t_abm_random, "abm_run_s": per_run_s,
+        "abm_agent_hours_per_s": keep * replicates * agents * (hours - 1) / t_abm_screened,
+        "flagged_for_abm_fallback": int(flagged.sum()),
+        "surrogate_peak_rel_err_median": float(np.median(peak_err)),
+        "surrogate_peak_within_5pct": float(np.mean(peak_err <= 0.05)),
+        "screened_best_param_err": float(unit_distance(cand[best][pick], hidden)[0]),
+        "screened_best_curve_mse": float(err_s[pick]),
+        "screened_best_peak_rel_err_vs_target": float(relative_peak_error(mean_s[pick:pick + 1], target[None], days)[0]),
+        "random_best_param_err": float(unit_distance(cand[rand_idx][pick_r], hidden)[0]),
+        "random_best_curve_mse": float(err_r[pick_r]),
+        "random_best_peak_rel_err_vs_target": float(relative_peak_error(mean_r[pick_r:pick_r + 1], target[None],
+                                                                         days)[0]),
+        "abm_only_sweep_s_estimated": abm_only_s, "screened_sweep_s": screened_s,
+        "sweep_speedup": abm_only_s / screened_s,
+    }
