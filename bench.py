@@ -187,6 +187,7 @@ def run_batched(args, stream, flush) -> dict:
     ens = Ensemble(params)
     build_s = time.perf_counter() - t0
     ens.set_stream(stream.cuda_stream)
+    shape = ens.autotune(24)
     ens.save_state()
     for _ in range(1):
         ens.restore_state()
@@ -232,6 +233,7 @@ def run_batched(args, stream, flush) -> dict:
             "sequential_plain_value": sequential_value, "sequential_sample": len(sample),
             "speedup_vs_sequential_plain": batched_value / sequential_value,
             "ms_per_step": ms_total / steps, "steps": steps, "world_build_and_upload_s": build_s,
+            "launch_shape": shape,
             "workload": "256 replicates, populations log-uniform in [10k, 500k], grid ceil(sqrt(N/0.16)), regular "
                         "rate U[0.02, 0.10], 0.05% exposed, 2400 h, no interventions, seeds from 11"}
 
@@ -281,6 +283,7 @@ def run_gpu(args, cfg):
 
     eng = Epidemiology(config, records=records)
     eng.set_stream(stream.cuda_stream)
+    shape = eng.autotune(24)  # launch shapes of the tick kernels (results do not depend on them)
     eng.save_state()
 
     def step():
@@ -344,6 +347,7 @@ def run_gpu(args, cfg):
         torch.cuda.synchronize()
         t0 = time.perf_counter()
         e = Epidemiology(config, records=host_records)
+        e.set_launch_shape(shape["decide_blocks"], shape["commit_slots"])
         r = e.run()
         e.close()
         e2e_ms += 1000.0 * (time.perf_counter() - t0)
@@ -354,6 +358,7 @@ def run_gpu(args, cfg):
     # carry CUDA event nodes around every kernel (on the engine's stream)
     prof = Epidemiology(config, records=records)
     prof.set_stream(stream.cuda_stream)
+    prof.set_launch_shape(shape["decide_blocks"], shape["commit_slots"])
     prof.set_profiling(True)
     prof.run()
     stats = prof.kernel_stats()
@@ -364,11 +369,12 @@ def run_gpu(args, cfg):
     alg_bytes = DECIDE_BYTES_PER_AGENT * n + cells
     achieved = alg_bytes / (avg_ms / 1000.0) / 1e9
     peak, peak_kind = _peaks()
-    traffic = None
-    tpath = os.path.join(ROOT, "profiles", "k_decide_traffic.json")
+    traffic = None  # DRAM bytes of one k_decide launch from the committed ncu capture
+    tpath = os.path.join(ROOT, "profiles", "k_decide_traffic.txt")
     if os.path.exists(tpath):
         with open(tpath) as f:
-            traffic = json.load(f).get("bytes_per_launch")
+            first = f.readline()
+        traffic = int(first.rsplit(":", 1)[1]) * n // 1_000_000  # captured at 1M agents; scales with agents
 
     batched = run_batched(args, stream, flush) if not args.no_batched else None
 
@@ -385,7 +391,7 @@ def run_gpu(args, cfg):
                                    "vaccination + hospital build (tests/golden/c2_small_pox_1m.json)",
                        "agents": n, "grid": G, "hours_per_step": hours_per_step, "parallelism": f"replicas{world}",
                        "l2": "flushed between steps (512 MiB write); inputs L2-resident within a step",
-                       "wall_s": wall},
+                       "launch_shape": shape, "wall_s": wall},
             "roofline": {"bound": "hbm", "kernel": "k_decide", "achieved": achieved, "peak": peak, "unit": "GB/s",
                          "frac": achieved / peak, "peak_kind": peak_kind, "traffic": traffic,
                          "alg_bytes_per_launch": alg_bytes, "avg_launch_ms": avg_ms,

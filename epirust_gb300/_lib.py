@@ -104,8 +104,13 @@ EXPORTS = [
     "epi_ensemble_create", "epi_ensemble_destroy", "epi_ensemble_last_error", "epi_ensemble_set_stream",
     "epi_ensemble_replicates", "epi_ensemble_run", "epi_ensemble_snapshot", "epi_ensemble_check",
     "epi_ensemble_save_state", "epi_ensemble_restore_state", "epi_ensemble_set_profiling", "epi_ensemble_kernel_stats",
-    "epi_ensemble_kernels_launched", "epi_ensemble_hour_bytes",
+    "epi_ensemble_kernels_launched", "epi_ensemble_hour_bytes", "epi_engine_autotune", "epi_engine_set_launch_shape",
+    "epi_engine_launch_shape", "epi_ensemble_autotune",
 ]
+
+
+class LaunchShape(C.Structure):
+    _fields_ = [("decide_blocks", C.c_uint32), ("commit_slots", C.c_uint32), ("hour_us", C.c_double)]
 
 # include/epi_surrogate.h
 MLP_EXPORTS = [
@@ -196,6 +201,10 @@ def lib():
     _sig(L, "epi_ensemble_kernels_launched", C.c_int, [V, P(C.c_uint64)])
     _sig(L, "epi_ensemble_hour_bytes", C.c_int, [V, C.c_uint32, P(C.c_double)])
     _sig(L, "epi_tick_hour_noalloc", C.c_int, [P(EpiParams), C.c_uint32, C.c_uint32, V, V, V, V, V, V, V, V])
+    _sig(L, "epi_engine_autotune", C.c_int, [V, C.c_uint32, P(LaunchShape)])
+    _sig(L, "epi_engine_set_launch_shape", C.c_int, [V, P(LaunchShape)])
+    _sig(L, "epi_engine_launch_shape", C.c_int, [V, P(LaunchShape)])
+    _sig(L, "epi_ensemble_autotune", C.c_int, [V, C.c_uint32, P(LaunchShape)])
     F = P(C.c_float)
     _sig(L, "epi_mlp_create", C.c_int, [P(MlpConfig), P(V)])
     _sig(L, "epi_mlp_destroy", C.c_int, [V])

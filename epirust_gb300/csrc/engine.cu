@@ -9,6 +9,7 @@
 #include <cuda_runtime.h>
 
 #include <algorithm>
+#include <chrono>
 #include <cstdio>
 #include <cstring>
 #include <map>
@@ -58,8 +59,10 @@ struct epi_engine {
     uint32_t slots = 0;        // agent slots (chunk-padded replicates)
     size_t plane_bytes = 0;    // all bordered byte planes
     size_t claim_cells = 0;    // all claim planes
-    int grid_blocks = 0;       // resident grid of the counting kernels
-    int commit_blocks = 0;     // one thread per slot
+    int grid_blocks = 0;       // grid of the counting kernels (k_decide, k_sleep)
+    int commit_slots = kCommitSlots;  // slots per k_commit thread (1, 2 or 4)
+    int commit_blocks = 0;
+    int resident_blocks = 0;   // SMs x resident k_decide blocks per SM
     // device
     DevParams* d_params = nullptr;
     uint32_t* d_chunk_rep = nullptr;  // null for a single replicate
@@ -282,8 +285,20 @@ static DecideKernel decide_kernel(uint32_t hod) {
     }
 }
 
-static int commit_blocks_for(uint32_t slots) {
-    return (int)std::max<uint32_t>(1u, (slots + kThreads * kCommitSlots - 1) / (kThreads * kCommitSlots));
+static int commit_blocks_for(uint32_t slots, int per_thread = kCommitSlots) {
+    const uint32_t per_block = kThreads * (uint32_t)per_thread;
+    return (int)std::max<uint32_t>(1u, (slots + per_block - 1) / per_block);
+}
+
+// k_commit with S slots per thread.
+using CommitKernel = void (*)(const DevParams*, const uint32_t*, uint32_t, uint32_t*, const uint32_t*, uint8_t*,
+                              const uint32_t*, const uint32_t*, const uint32_t*, uint32_t);
+static CommitKernel commit_kernel(int slots_per_thread) {
+    switch (slots_per_thread) {
+        case 1: return k_commit<1>;
+        case 2: return k_commit<2>;
+        default: return k_commit<4>;
+    }
 }
 // Kernels of hours hour_base .. hour_base + nh - 1 (hour_base read on the device).
 // Offset within the segment of the first hour that opens a new claim window, or nh; later
@@ -310,10 +325,11 @@ static int enqueue_hours(epi_engine* h, uint32_t first_hour, uint32_t nh) {
             LAUNCH(kKDecide, (decide<<<h->grid_blocks, kThreads, 0, h->stream>>>(
                                   h->d_params, h->d_chunk_rep, n_chunks, h->d_pos, h->d_st, h->d_home, h->d_work, h->d_wsa,
                                   h->d_plane, h->d_claim, h->d_tgt, h->d_lost, rows, h->d_hour_base, k, h->d_err)));
-            LAUNCH(kKCommit, (k_commit<<<h->commit_blocks, kThreads, 0, h->stream>>>(h->d_params, h->d_chunk_rep, h->slots,
-                                                                                     h->d_pos, h->d_tgt, h->d_plane,
-                                                                                     h->d_claim, h->d_lost, h->d_hour_base,
-                                                                                     k)));
+            const CommitKernel commit = commit_kernel(h->commit_slots);
+            LAUNCH(kKCommit, (commit<<<h->commit_blocks, kThreads, 0, h->stream>>>(h->d_params, h->d_chunk_rep, h->slots,
+                                                                                   h->d_pos, h->d_tgt, h->d_plane,
+                                                                                   h->d_claim, h->d_lost, h->d_hour_base,
+                                                                                   k)));
         }
     }
     CK(cudaMemcpyAsync(h->h_counts, h->d_counts, (size_t)nh * row_words * sizeof(uint32_t), cudaMemcpyDeviceToHost,
@@ -636,8 +652,9 @@ static int engine_init(epi_engine* h, const epi_params* params, const epi_agent_
     CK(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_decide<kHcMove>, kThreads, 0));
     per_sm = std::max(per_sm, 1);
     const uint64_t n_chunks = slots / kChunk;
-    h->grid_blocks = (int)std::min<uint64_t>(n_chunks, (uint64_t)sms * per_sm);
-    h->commit_blocks = commit_blocks_for(h->slots);
+    h->resident_blocks = sms * per_sm;
+    h->grid_blocks = (int)std::min<uint64_t>(n_chunks, (uint64_t)h->resident_blocks);
+    h->commit_blocks = commit_blocks_for(h->slots, h->commit_slots);
     CK(cudaStreamCreateWithFlags(&h->stream, cudaStreamNonBlocking));
     h->own_stream = true;
     CK(cudaMalloc(&h->d_params, R * sizeof(DevParams)));
@@ -782,6 +799,76 @@ static int check_all(epi_engine* h) {
         h->err = "invariants: " + std::to_string(v[0]) + " agents off their cell class, " + std::to_string(v[1]) +
                  " occupied cells for " + std::to_string(population) + " agents";
         return EPI_ERR_INVARIANT;
+    }
+    return EPI_OK;
+}
+
+static int save_state(epi_engine* h);
+static int restore_state(epi_engine* h);
+
+static int set_launch_shape(epi_engine* h, uint32_t decide_blocks, uint32_t commit_slots) {
+    const uint32_t n_chunks = h->slots / kChunk;
+    if (decide_blocks == 0 || decide_blocks > n_chunks || !(commit_slots == 1 || commit_slots == 2 || commit_slots == 4)) {
+        h->err = "launch shape: k_decide blocks in [1, " + std::to_string(n_chunks) + "], k_commit slots 1, 2 or 4";
+        return EPI_ERR_ARG;
+    }
+    CK(cudaStreamSynchronize(h->stream));
+    h->grid_blocks = (int)decide_blocks;
+    h->commit_slots = (int)commit_slots;
+    h->commit_blocks = commit_blocks_for(h->slots, h->commit_slots);
+    destroy_graphs(h);  // they bake the launch shapes in
+    return EPI_OK;
+}
+
+// Launch-shape autotuner: times hours 1..hours of the engine's current world under each
+// candidate (k_decide grid: the resident grid, twice it, one chunk per block; k_commit: 1, 2
+// or 4 slots per thread), restarting every candidate from the same state, and keeps the
+// fastest.  Results do not depend on the shape; the state, the run's rows and the launch
+// counter are restored afterwards (the saved checkpoint is replaced).
+static int autotune(epi_engine* h, uint32_t hours, epi_launch_shape* out) {
+    if (hours == 0 || hours > 24u * 7u) { h->err = "autotune hours must be in [1, 168]"; return EPI_ERR_ARG; }
+    const uint32_t n_chunks = h->slots / kChunk;
+    std::vector<uint32_t> grids;
+    const uint64_t cand[3] = {(uint64_t)h->resident_blocks, 2ull * (uint64_t)h->resident_blocks, (uint64_t)n_chunks};
+    for (uint64_t g : cand) {
+        const uint32_t v = (uint32_t)std::max<uint64_t>(1, std::min<uint64_t>(g, n_chunks));
+        if (std::find(grids.begin(), grids.end(), v) == grids.end()) grids.push_back(v);
+    }
+    const bool prof = h->profiling;
+    const uint64_t launched = h->kernels_launched;
+    h->profiling = false;
+    int rc = save_state(h);
+    if (rc) return rc;
+    double best = 1e300;
+    uint32_t best_g = (uint32_t)h->grid_blocks, best_c = (uint32_t)h->commit_slots;
+    for (uint32_t g : grids) {
+        const uint32_t slots[3] = {1u, 2u, 4u};
+        for (uint32_t c : slots) {
+            rc = set_launch_shape(h, g, c);
+            double t_min = 1e300;
+            for (int rep = 0; rep < 3 && !rc; ++rep) {  // the first pass captures the graphs
+                rc = restore_state(h);
+                if (rc) break;
+                const auto t0 = std::chrono::steady_clock::now();
+                rc = run_hours(h, 1, hours);
+                const double t = std::chrono::duration<double>(std::chrono::steady_clock::now() - t0).count();
+                if (rep > 0) t_min = std::min(t_min, t);
+            }
+            if (rc) break;
+            if (t_min < best) { best = t_min; best_g = g; best_c = c; }
+        }
+        if (rc) break;
+    }
+    h->profiling = prof;
+    int rc2 = set_launch_shape(h, best_g, best_c);
+    if (!rc2) rc2 = restore_state(h);
+    h->kernels_launched = launched;
+    if (rc) return rc;
+    if (rc2) return rc2;
+    if (out) {
+        out->decide_blocks = best_g;
+        out->commit_slots = best_c;
+        out->hour_us = best * 1e6 / hours;
     }
     return EPI_OK;
 }
@@ -1038,6 +1125,23 @@ int epi_engine_check(epi_engine* h) { return h ? check_all(h) : EPI_ERR_ARG; }
 int epi_engine_save_state(epi_engine* h) { return h ? save_state(h) : EPI_ERR_ARG; }
 int epi_engine_restore_state(epi_engine* h) { return h ? restore_state(h) : EPI_ERR_ARG; }
 
+int epi_engine_autotune(epi_engine* h, uint32_t hours, epi_launch_shape* chosen) {
+    return h ? autotune(h, hours, chosen) : EPI_ERR_ARG;
+}
+
+int epi_engine_set_launch_shape(epi_engine* h, const epi_launch_shape* shape) {
+    if (!h || !shape) return EPI_ERR_ARG;
+    return set_launch_shape(h, shape->decide_blocks, shape->commit_slots);
+}
+
+int epi_engine_launch_shape(const epi_engine* h, epi_launch_shape* out) {
+    if (!h || !out) return EPI_ERR_ARG;
+    out->decide_blocks = (uint32_t)h->grid_blocks;
+    out->commit_slots = (uint32_t)h->commit_slots;
+    out->hour_us = 0.0;
+    return EPI_OK;
+}
+
 int epi_engine_kernels_launched(const epi_engine* h, uint64_t* out) {
     if (!h || !out) return EPI_ERR_ARG;
     *out = h->kernels_launched;
@@ -1156,6 +1260,10 @@ int epi_ensemble_set_profiling(epi_ensemble* e, int on) { return e ? epi_engine_
 
 int epi_ensemble_kernel_stats(const epi_ensemble* e, uint32_t* launches, double* total_ms, int n) {
     return e ? epi_engine_kernel_stats(&e->core, launches, total_ms, n) : EPI_ERR_ARG;
+}
+
+int epi_ensemble_autotune(epi_ensemble* e, uint32_t hours, epi_launch_shape* chosen) {
+    return e ? autotune(&e->core, hours, chosen) : EPI_ERR_ARG;
 }
 
 int epi_ensemble_kernels_launched(const epi_ensemble* e, uint64_t* out) {
@@ -1282,7 +1390,7 @@ extern "C" int epi_tick_hour_noalloc(const epi_params* params, uint32_t hour, ui
         const DecideKernel decide = decide_kernel(hod);
         decide<<<blocks, kThreads, 0, s>>>(d_params, nullptr, n_chunks, pos, st, home, work, work_start_at, plane, d_claim,
                                            d_tgt, nullptr, counts, d_hour, 0u, d_err);
-        k_commit<<<commit_blocks_for(n), kThreads, 0, s>>>(d_params, nullptr, n, pos, d_tgt, plane, d_claim, nullptr,
+        k_commit<kCommitSlots><<<commit_blocks_for(n), kThreads, 0, s>>>(d_params, nullptr, n, pos, d_tgt, plane, d_claim, nullptr,
                                                            d_hour, 0u);
     }
     NOALLOC_CK(cudaGetLastError());

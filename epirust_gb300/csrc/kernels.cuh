@@ -208,9 +208,11 @@ __global__ void __launch_bounds__(kThreads) k_decide(const DevParams* __restrict
 // (the serial resolve of allocation_map.rs:93-102 in index order), others keep their cell.
 // With loss marks (lost != nullptr) a mover wins unless k_decide marked it beaten this
 // hour; without them the winner is read from the claim plane.  Each thread takes
-// kCommitSlots slots a block-width apart, issuing all their independent loads first.
-constexpr int kCommitSlots = 4;
+// S slots a block-width apart (S chosen by the launch-shape autotuner), issuing all their
+// independent loads first.
+constexpr int kCommitSlots = 4;  // default S
 
+template <int S>
 __global__ void __launch_bounds__(kThreads) k_commit(const DevParams* __restrict__ Pall, const uint32_t* __restrict__ chunk_rep,
                                                      uint32_t n_slots, uint32_t* __restrict__ pos,
                                                      const uint32_t* __restrict__ tgt, uint8_t* __restrict__ plane,
@@ -218,19 +220,19 @@ __global__ void __launch_bounds__(kThreads) k_commit(const DevParams* __restrict
                                                      const uint32_t* __restrict__ lost,
                                                      const uint32_t* __restrict__ hour_base, uint32_t hour_offset) {
     const uint32_t hour = *hour_base + hour_offset;
-    const uint32_t base = blockIdx.x * (blockDim.x * kCommitSlots) + threadIdx.x;
-    uint32_t t[kCommitSlots], p[kCommitSlots], l[kCommitSlots];
+    const uint32_t base = blockIdx.x * (blockDim.x * S) + threadIdx.x;
+    uint32_t t[S], p[S], l[S];
 #pragma unroll
-    for (int k = 0; k < kCommitSlots; ++k) {
+    for (int k = 0; k < S; ++k) {
         const uint32_t slot = base + k * blockDim.x;
         t[k] = slot < n_slots ? tgt[slot] : kNoAction;
         p[k] = slot < n_slots ? pos[slot] : 0u;
         l[k] = lost && slot < n_slots ? lost[slot] : 0u;
     }
-    const DevParams* Pr[kCommitSlots];
-    uint32_t won[kCommitSlots];
+    const DevParams* Pr[S];
+    uint32_t won[S];
 #pragma unroll
-    for (int k = 0; k < kCommitSlots; ++k) {
+    for (int k = 0; k < S; ++k) {
         const uint32_t slot = base + k * blockDim.x;
         Pr[k] = Pall + (chunk_rep && t[k] != kNoAction ? chunk_rep[slot / kChunk] : 0u);
         won[k] = kNoClaim;  // never equal to a key: stays put
@@ -241,7 +243,7 @@ __global__ void __launch_bounds__(kThreads) k_commit(const DevParams* __restrict
         }
     }
 #pragma unroll
-    for (int k = 0; k < kCommitSlots; ++k) {
+    for (int k = 0; k < S; ++k) {
         if (t[k] == kNoAction) continue;
         const DevParams& P = *Pr[k];
         if (!P.active) continue;

@@ -217,6 +217,21 @@ class Epidemiology:
         check(lib().epi_engine_kernels_launched(self._h, C.byref(v)), self._h)
         return v.value
 
+    def autotune(self, hours: int = 24) -> dict:
+        """Pick the fastest launch shape over hours 1..hours (state restored afterwards)."""
+        s = _lib.LaunchShape()
+        check(lib().epi_engine_autotune(self._h, hours, C.byref(s)), self._h)
+        return {"decide_blocks": s.decide_blocks, "commit_slots": s.commit_slots, "hour_us": s.hour_us}
+
+    def set_launch_shape(self, decide_blocks: int, commit_slots: int) -> None:
+        s = _lib.LaunchShape(decide_blocks, commit_slots, 0.0)
+        check(lib().epi_engine_set_launch_shape(self._h, C.byref(s)), self._h)
+
+    def launch_shape(self) -> dict:
+        s = _lib.LaunchShape()
+        check(lib().epi_engine_launch_shape(self._h, C.byref(s)), self._h)
+        return {"decide_blocks": s.decide_blocks, "commit_slots": s.commit_slots}
+
     def hour_bytes(self, hour: int) -> float:
         b = C.c_double(0.0)
         check(lib().epi_engine_hour_bytes(self._h, hour, C.byref(b)), self._h)
@@ -291,6 +306,12 @@ class Ensemble:
         v = C.c_uint64(0)
         self._check(lib().epi_ensemble_kernels_launched(self._h, C.byref(v)))
         return v.value
+
+    def autotune(self, hours: int = 24) -> dict:
+        """Pick the fastest launch shape for all replicates over hours 1..hours."""
+        s = _lib.LaunchShape()
+        self._check(lib().epi_ensemble_autotune(self._h, hours, C.byref(s)))
+        return {"decide_blocks": s.decide_blocks, "commit_slots": s.commit_slots, "hour_us": s.hour_us}
 
     def hour_bytes(self, hour: int) -> float:
         b = C.c_double(0.0)

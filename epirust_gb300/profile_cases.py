@@ -1,0 +1,96 @@
+"""Small, fixed workloads for profilers (ncu) and quick timing: each runs one hot path of the
+package and exits.
+
+    python -m epirust_gb300.profile_cases tick --agents 1000000 --grid 2500 --hours 48
+        the config-2 world (tests/golden/c2_small_pox_1m.json) resized, hours 1..hours-1
+        through simulate_hours (one CUDA graph per call); --events adds CUDA events per kernel
+    python -m epirust_gb300.profile_cases mlp-train --steps 30
+        the surrogate network 8 -> 512 x 3 -> 600, batch 256, on a seeded synthetic set of
+        4,096 samples: `steps` Adam steps (one graph replay each)
+    python -m epirust_gb300.profile_cases mlp-screen --candidates 65536
+        one network scoring `candidates` parameter vectors against a curve
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import os
+import time
+
+import numpy as np
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+C2 = os.path.join(os.path.dirname(HERE), "tests", "golden", "c2_small_pox_1m.json")
+
+
+def tick(args) -> dict:
+    from .engine import Config, Epidemiology
+
+    with open(C2) as f:
+        cfg = json.load(f)
+    cfg["population"]["Auto"]["number_of_agents"] = args.agents
+    cfg["geography_parameters"]["grid_size"] = args.grid
+    eng = Epidemiology(Config(json.dumps(cfg)))
+    eng.set_profiling(args.events)
+    t0 = time.perf_counter()
+    eng.simulate_hours(1, args.hours - 1)
+    dt = time.perf_counter() - t0
+    out = {"hours": args.hours - 1, "s": dt, "agent_hours_per_s": args.agents * (args.hours - 1) / dt}
+    if args.events:
+        out["kernels"] = {k: v for k, v in eng.kernel_stats().items() if v[0]}
+    eng.close()
+    return out
+
+
+def _net():
+    from .surrogate import Surrogate
+
+    return Surrogate(in_dim=8, out_dim=600, hidden=512, hidden_layers=3, batch=256, seed=1)
+
+
+def mlp_train(args) -> dict:
+    rng = np.random.default_rng(0)
+    x = rng.random((4096, 8))
+    y = np.sin(x @ rng.normal(size=(8, 600))) * 0.5
+    net = _net()
+    net.set_dataset(x, y)
+    t0 = time.perf_counter()
+    losses = net.train(args.steps, seed=0)
+    dt = time.perf_counter() - t0
+    net.close()
+    return {"steps": args.steps, "s": dt, "ms_per_step": 1000 * dt / max(args.steps, 1),
+            "first_loss": float(losses[0]), "last_loss": float(losses[-1])}
+
+
+def mlp_screen(args) -> dict:
+    rng = np.random.default_rng(1)
+    net = _net()
+    cand = rng.random((args.candidates, 8))
+    target = rng.random(600)
+    net.score(cand[:1024], target)  # warm-up (buffers, tensor maps)
+    t0 = time.perf_counter()
+    s = net.score(cand, target)
+    dt = time.perf_counter() - t0
+    net.close()
+    return {"candidates": args.candidates, "s": dt, "best": float(s.min())}
+
+
+def main() -> None:
+    ap = argparse.ArgumentParser(description=__doc__, formatter_class=argparse.RawDescriptionHelpFormatter)
+    sub = ap.add_subparsers(dest="case", required=True)
+    t = sub.add_parser("tick")
+    t.add_argument("--agents", type=int, default=1_000_000)
+    t.add_argument("--grid", type=int, default=2500)
+    t.add_argument("--hours", type=int, default=48)
+    t.add_argument("--events", action="store_true")
+    m = sub.add_parser("mlp-train")
+    m.add_argument("--steps", type=int, default=30)
+    s = sub.add_parser("mlp-screen")
+    s.add_argument("--candidates", type=int, default=65536)
+    args = ap.parse_args()
+    fn = {"tick": tick, "mlp-train": mlp_train, "mlp-screen": mlp_screen}[args.case]
+    print(json.dumps(fn(args)))
+
+
+if __name__ == "__main__":
+    main()

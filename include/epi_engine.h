@@ -250,6 +250,23 @@ int epi_engine_restore_state(epi_engine* h);
 /* Number of engine kernels launched so far on this handle (graph nodes included). */
 int epi_engine_kernels_launched(const epi_engine* h, uint64_t* out);
 
+/* Launch shape of the tick kernels: the k_decide / k_sleep grid and the agents per k_commit
+ * thread.  Results never depend on it. */
+typedef struct {
+    uint32_t decide_blocks;  /* 1 .. number of 256-agent chunks */
+    uint32_t commit_slots;   /* 1, 2 or 4 */
+    double hour_us;          /* autotune: mean wall time of a simulated hour with this shape */
+} epi_launch_shape;
+
+/* Autotuner (no reference counterpart): time hours 1..hours (<= 168) of the current world
+ * under each candidate shape -- k_decide grid = resident blocks, twice that, or one chunk per
+ * block; 1, 2 or 4 agents per k_commit thread -- from the same starting state, keep the
+ * fastest and restore the state.  Call it before simulating; it replaces the checkpoint of
+ * epi_engine_save_state. */
+int epi_engine_autotune(epi_engine* h, uint32_t hours, epi_launch_shape* chosen);
+int epi_engine_set_launch_shape(epi_engine* h, const epi_launch_shape* shape);
+int epi_engine_launch_shape(const epi_engine* h, epi_launch_shape* out);
+
 /* Kernel timing: when enabled, every kernel launch of the engine is bracketed by CUDA
  * events on the launching stream and CUDA graphs are not used.  kernel_stats returns, per
  * kernel kind k < n, its launch count and total milliseconds; names via kernel_name. */
@@ -291,6 +308,8 @@ int epi_ensemble_restore_state(epi_ensemble* e);
 int epi_ensemble_set_profiling(epi_ensemble* e, int on);
 int epi_ensemble_kernel_stats(const epi_ensemble* e, uint32_t* launches, double* total_ms, int n);
 int epi_ensemble_kernels_launched(const epi_ensemble* e, uint64_t* out);
+/* epi_engine_autotune for all replicates together. */
+int epi_ensemble_autotune(epi_ensemble* e, uint32_t hours, epi_launch_shape* chosen);
 int epi_ensemble_hour_bytes(const epi_ensemble* e, uint32_t hour, double* bytes);
 
 /* ---------------------------------------------------------------- no-allocation hour */
