@@ -110,6 +110,23 @@ def _dist():
     return world, rank, local
 
 
+def aggregate_replicas(ms_total: float, agent_hours: float, device: str = "cpu") -> tuple[float, float]:
+    """Replicas only: the job's time is the slowest rank's, its work the sum over ranks."""
+    import torch
+    import torch.distributed as dist
+
+    t = torch.tensor([ms_total, agent_hours], dtype=torch.float64, device=device)
+    ms_max = t[0].clone()
+    dist.all_reduce(ms_max, op=dist.ReduceOp.MAX)
+    dist.all_reduce(t[1:], op=dist.ReduceOp.SUM)
+    return float(ms_max), float(t[1])
+
+
+def replica_seed(seed: int, rank: int) -> int:
+    """Every rank simulates an independent world."""
+    return seed + 1000 * rank
+
+
 def _agent_hours(rows, n_agents: int) -> float:
     return float(n_agents) * float(len(rows))
 
@@ -271,7 +288,7 @@ def run_gpu(args, cfg):
     torch.cuda.set_device(local)
     dev_index = torch.cuda.current_device()
     cfg = dict(cfg)
-    cfg["seed"] = int(cfg.get("seed", 0)) + 1000 * rank  # independent replicas
+    cfg["seed"] = replica_seed(int(cfg.get("seed", 0)), rank)
     config = Config(json.dumps(cfg))
     n = config.number_of_agents
     G = config.params.grid_size
@@ -327,13 +344,7 @@ def run_gpu(args, cfg):
     hours_per_step = len(rows)
 
     if world > 1:
-        import torch.distributed as dist
-
-        t = torch.tensor([ms_total, agent_hours], dtype=torch.float64, device="cuda")
-        ms_max = t[0].clone()
-        dist.all_reduce(ms_max, op=dist.ReduceOp.MAX)
-        dist.all_reduce(t[1:], op=dist.ReduceOp.SUM)
-        ms_total, agent_hours = float(ms_max), float(t[1])
+        ms_total, agent_hours = aggregate_replicas(ms_total, agent_hours, "cuda")
     value = agent_hours / (ms_total / 1000.0)
 
     # ---- e2e: host records -> create (upload) -> run -> counts on the host -> destroy
