@@ -305,6 +305,15 @@ __device__ __forceinline__ Cell perform_movements(const DevParams& P, const Plan
     } else {
         const Rect cur = area_rect(P, st_area(s), home, work);
         const bool worker = ws != EPI_WS_NA;  // Normal or Essential here
+        if (HC != kHcMove) {
+            // Both work-status arms below draw from the movement block whenever the agent
+            // moves at all; materialising it here, before the branch, runs the Philox rounds
+            // once per warp instead of once per arm.  (Draws are pure functions of the
+            // counter: an unused block changes nothing.)
+            const uint32_t v = s & kStateMask;
+            const bool override_home = HC == kHcHome && worker && (v == EPI_I_MILD || v == EPI_I_SEVERE);
+            if (can_move(s) || override_home) (void)dr.m(0);
+        }
         if (HC == kHcMove) {
             nc = move_agent_from(pl, s, cur, cell, dr);
         } else if (HC == kHcTransport) {
