@@ -179,7 +179,6 @@ __global__ void __launch_bounds__(kThreads) k_decide(const DevParams* __restrict
             const uint32_t key = claim_key(hour, i);
             const uint32_t old = moving ? atomicMin(&rclaim[(size_t)nc.y * P.W + nc.x], key) : kNoClaim;
             if (infect) infection_dynamics(P, pl, s, at, area_rect(P, st_area(s), hm, wk), nc, hour, dr);
-            const uint32_t cls = cell_class(P, s);
             if (moving) {
                 // The claim that atomicMin finds names an agent this one competes with: of
                 // the two the higher index loses.  Every claimant but the cell's lowest is
@@ -195,7 +194,13 @@ __global__ void __launch_bounds__(kThreads) k_decide(const DevParams* __restrict
                     }
                 }
             }
-            tgt[slot] = (moving || cls != cell_class(P, s0)) ? encode_target(nc, cls) : kNoAction;
+            // the plane byte changes when the agent moves or its class changes (s == s0 keeps it)
+            uint32_t t = kNoAction;
+            if (moving || s != s0) {
+                const uint32_t cls = cell_class(P, s);
+                if (moving || cls != cell_class(P, s0)) t = encode_target(nc, cls);
+            }
+            tgt[slot] = t;
             if (s != s0 || at != at0) st[slot] = make_uint2(s, at);
             bin = count_bin(s);
         }

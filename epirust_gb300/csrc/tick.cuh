@@ -87,13 +87,17 @@ __device__ __forceinline__ uint32_t high_mask(const Rows3& r) {
 }
 
 // Neighbours of (x, y) inside area a and the grid (Area::get_neighbors_of filtered by
-// is_point_in_grid), as a mask in NeighborIterator order.
+// is_point_in_grid), as a mask in NeighborIterator order: three column and three row tests
+// (each one unsigned range compare) combined row by row.
 __device__ __forceinline__ uint32_t valid_neighbours(const Rect& a, int32_t G, int32_t x, int32_t y) {
     const int32_t lx = max(a.x0, 0), hx = min(a.x1, G - 1), ly = max(a.y0, 0), hy = min(a.y1, G - 1);
-    const uint32_t cl = (x - 1 >= lx) & (x - 1 <= hx), cc = (x >= lx) & (x <= hx), cr = (x + 1 >= lx) & (x + 1 <= hx);
-    const uint32_t rt = (y - 1 >= ly) & (y - 1 <= hy), rm = (y >= ly) & (y <= hy), rb = (y + 1 >= ly) & (y + 1 <= hy);
-    return (cl & rt) | ((cc & rt) << 1) | ((cr & rt) << 2) | ((cl & rm) << 3) | ((cr & rm) << 4) | ((cl & rb) << 5) |
-           ((cc & rb) << 6) | ((cr & rb) << 7);
+    if (hx < lx || hy < ly) return 0u;
+    const uint32_t wx = (uint32_t)(hx - lx), wy = (uint32_t)(hy - ly);
+    const uint32_t dx = (uint32_t)(x - 1 - lx), dy = (uint32_t)(y - 1 - ly);
+    const uint32_t C = (uint32_t)(dx <= wx) | ((uint32_t)(dx + 1u <= wx) << 1) | ((uint32_t)(dx + 2u <= wx) << 2);
+    const uint32_t top = (dy <= wy) ? C : 0u, bot = (dy + 2u <= wy) ? C : 0u;
+    const uint32_t mid = (dy + 1u <= wy) ? ((C & 1u) | ((C >> 1) & 2u)) : 0u;
+    return top | (mid << 3) | (bot << 5);
 }
 
 // Position of the j-th set bit (j counted from 0, j < popc(m)) of an 8-bit mask.
