@@ -70,6 +70,7 @@ struct epi_engine {
     uint32_t* d_lost = nullptr;  // per slot: the hour in which the agent's claim was beaten
     uint2* d_st = nullptr;
     uint8_t* d_plane = nullptr;
+    uint8_t* d_danger = nullptr;  // infectious-neighbour counts, same layout as d_plane
     uint32_t* d_claim = nullptr;
     uint32_t* d_counts = nullptr;  // [hour of segment][replicate][8]
     uint32_t* d_hour_base = nullptr;
@@ -101,6 +102,7 @@ struct epi_engine {
     uint32_t *s_pos = nullptr, *s_wsa = nullptr;
     uint2* s_st = nullptr;
     uint8_t* s_plane = nullptr;
+    uint8_t* s_danger = nullptr;
     bool saved = false;
 
     uint32_t R() const { return (uint32_t)reps.size(); }
@@ -260,8 +262,8 @@ static int ensure_counts(epi_engine* h, uint32_t hours_needed) {
 
 // ------------------------------------------------------------------ the hour loop
 using DecideKernel = void (*)(const DevParams*, const uint32_t*, uint32_t, const uint32_t*, uint2*, const uint32_t*,
-                              const uint32_t*, uint32_t*, const uint8_t*, uint32_t*, uint32_t*, uint32_t*, uint32_t*,
-                              const uint32_t*, uint32_t, int*);
+                              const uint32_t*, uint32_t*, const uint8_t*, const uint8_t*, uint32_t*, uint32_t*, uint32_t*,
+                              uint32_t*, const uint32_t*, uint32_t, int*);
 
 // Hours 2..6 of a day change nothing once hour 1 has sent everyone but hospital staff home
 // (routine, citizen/mod.rs:243-247, sets current_area = home_location and nothing else), so
@@ -292,7 +294,7 @@ static int commit_blocks_for(uint32_t slots, int per_thread = kCommitSlots) {
 
 // k_commit with S slots per thread.
 using CommitKernel = void (*)(const DevParams*, const uint32_t*, uint32_t, uint32_t*, const uint32_t*, uint8_t*,
-                              const uint32_t*, const uint32_t*, const uint32_t*, uint32_t);
+                              uint8_t*, const uint32_t*, const uint32_t*, const uint32_t*, uint32_t);
 static CommitKernel commit_kernel(int slots_per_thread) {
     switch (slots_per_thread) {
         case 1: return k_commit<1>;
@@ -324,10 +326,11 @@ static int enqueue_hours(epi_engine* h, uint32_t first_hour, uint32_t nh) {
             const DecideKernel decide = decide_kernel(hod);
             LAUNCH(kKDecide, (decide<<<h->grid_blocks, kThreads, 0, h->stream>>>(
                                   h->d_params, h->d_chunk_rep, n_chunks, h->d_pos, h->d_st, h->d_home, h->d_work, h->d_wsa,
-                                  h->d_plane, h->d_claim, h->d_tgt, h->d_lost, rows, h->d_hour_base, k, h->d_err)));
+                                  h->d_plane, h->d_danger, h->d_claim, h->d_tgt, h->d_lost, rows, h->d_hour_base, k,
+                                  h->d_err)));
             const CommitKernel commit = commit_kernel(h->commit_slots);
             LAUNCH(kKCommit, (commit<<<h->commit_blocks, kThreads, 0, h->stream>>>(h->d_params, h->d_chunk_rep, h->slots,
-                                                                                   h->d_pos, h->d_tgt, h->d_plane,
+                                                                                   h->d_pos, h->d_tgt, h->d_plane, h->d_danger,
                                                                                    h->d_claim, h->d_lost, h->d_hour_base,
                                                                                    k)));
         }
@@ -561,9 +564,9 @@ static int run_loop_body(epi_engine* h) {
 static void free_device(epi_engine* h) {
     destroy_graphs(h);
     cudaFree(h->d_params); cudaFree(h->d_chunk_rep); cudaFree(h->d_pos); cudaFree(h->d_home); cudaFree(h->d_work);
-    cudaFree(h->d_wsa); cudaFree(h->d_tgt); cudaFree(h->d_lost); cudaFree(h->d_st); cudaFree(h->d_plane); cudaFree(h->d_claim);
+    cudaFree(h->d_wsa); cudaFree(h->d_tgt); cudaFree(h->d_lost); cudaFree(h->d_st); cudaFree(h->d_plane); cudaFree(h->d_danger); cudaFree(h->d_claim);
     cudaFree(h->d_counts); cudaFree(h->d_hour_base); cudaFree(h->d_err); cudaFree(h->d_scratch);
-    cudaFree(h->s_pos); cudaFree(h->s_wsa); cudaFree(h->s_st); cudaFree(h->s_plane);
+    cudaFree(h->s_pos); cudaFree(h->s_wsa); cudaFree(h->s_st); cudaFree(h->s_plane); cudaFree(h->s_danger);
     if (h->h_counts) cudaFreeHost(h->h_counts);
     if (h->h_hour_base) cudaFreeHost(h->h_hour_base);
     for (auto& pe : h->pending)
@@ -676,6 +679,7 @@ static int engine_init(epi_engine* h, const epi_params* params, const epi_agent_
     CK(cudaMalloc(&h->d_lost, slots * sizeof(uint32_t)));
     CK(cudaMalloc(&h->d_st, slots * sizeof(uint2)));
     CK(cudaMalloc(&h->d_plane, h->plane_bytes));
+    CK(cudaMalloc(&h->d_danger, h->plane_bytes));
     CK(cudaMalloc(&h->d_claim, h->claim_cells * sizeof(uint32_t)));
     CK(cudaMalloc(&h->d_hour_base, sizeof(uint32_t)));
     CK(cudaMalloc(&h->d_err, sizeof(int)));
@@ -706,12 +710,14 @@ static int engine_init(epi_engine* h, const epi_params* params, const epi_agent_
     CK(cudaMemsetAsync(h->d_tgt, 0xFF, slots * sizeof(uint32_t), h->stream));
     CK(cudaMemsetAsync(h->d_lost, 0xFF, slots * sizeof(uint32_t), h->stream));
     CK(cudaMemsetAsync(h->d_plane, 0, h->plane_bytes, h->stream));
+    CK(cudaMemsetAsync(h->d_danger, 0, h->plane_bytes, h->stream));
     CK(cudaMemsetAsync(h->d_claim, 0xFF, h->claim_cells * sizeof(uint32_t), h->stream));
     CK(cudaMemsetAsync(h->d_err, 0, sizeof(int), h->stream));
     rc = push_params(h);
     if (rc) return rc;
     LAUNCH(kKBuildPlane, (k_build_plane<<<blocks_for(h->slots), kThreads, 0, h->stream>>>(
-                              h->d_params, h->d_chunk_rep, h->slots, h->d_pos, h->d_st, h->d_plane, h->d_err)));
+                              h->d_params, h->d_chunk_rep, h->slots, h->d_pos, h->d_st, h->d_plane, h->d_danger,
+                              h->d_err)));
     CK(cudaStreamSynchronize(h->stream));  // the host mirrors go out of scope
     rc = harvest_events(h);
     if (rc) return rc;
@@ -788,6 +794,8 @@ static int check_all(epi_engine* h) {
                          h->d_params, h->d_chunk_rep, h->slots, h->d_pos, h->d_st, h->d_plane, h->d_scratch)));
     LAUNCH(kKCheck, (k_check_plane<<<h->grid_blocks, kThreads, 0, h->stream>>>(h->plane_bytes, h->d_plane,
                                                                                 h->d_scratch + 1)));
+    LAUNCH(kKCheck, (k_check_danger<<<dim3(64, std::min<uint32_t>(h->R(), 4096u)), kThreads, 0, h->stream>>>(
+                         h->d_params, h->R(), h->d_plane, h->d_danger, h->d_scratch + 2)));
     unsigned long long v[4] = {0, 0, 0, 0};
     CK(cudaMemcpyAsync(v, h->d_scratch, sizeof v, cudaMemcpyDeviceToHost, h->stream));
     CK(cudaStreamSynchronize(h->stream));
@@ -795,9 +803,10 @@ static int check_all(epi_engine* h) {
     if (rc) return rc;
     uint64_t population = 0;
     for (const auto& rep : h->reps) population += rep.n;
-    if (v[0] || v[1] != population) {
+    if (v[0] || v[1] != population || v[2]) {
         h->err = "invariants: " + std::to_string(v[0]) + " agents off their cell class, " + std::to_string(v[1]) +
-                 " occupied cells for " + std::to_string(population) + " agents";
+                 " occupied cells for " + std::to_string(population) + " agents, " + std::to_string(v[2]) +
+                 " cells with a wrong infectious-neighbour count";
         return EPI_ERR_INVARIANT;
     }
     return EPI_OK;
@@ -880,11 +889,13 @@ static int save_state(epi_engine* h) {
         CK(cudaMalloc(&h->s_wsa, n * sizeof(uint32_t)));
         CK(cudaMalloc(&h->s_st, n * sizeof(uint2)));
         CK(cudaMalloc(&h->s_plane, h->plane_bytes));
+        CK(cudaMalloc(&h->s_danger, h->plane_bytes));
     }
     CK(cudaMemcpyAsync(h->s_pos, h->d_pos, n * sizeof(uint32_t), cudaMemcpyDeviceToDevice, h->stream));
     CK(cudaMemcpyAsync(h->s_wsa, h->d_wsa, n * sizeof(uint32_t), cudaMemcpyDeviceToDevice, h->stream));
     CK(cudaMemcpyAsync(h->s_st, h->d_st, n * sizeof(uint2), cudaMemcpyDeviceToDevice, h->stream));
     CK(cudaMemcpyAsync(h->s_plane, h->d_plane, h->plane_bytes, cudaMemcpyDeviceToDevice, h->stream));
+    CK(cudaMemcpyAsync(h->s_danger, h->d_danger, h->plane_bytes, cudaMemcpyDeviceToDevice, h->stream));
     CK(cudaStreamSynchronize(h->stream));
     for (auto& rep : h->reps) {
         rep.s_iv = rep.iv;
@@ -903,6 +914,7 @@ static int restore_state(epi_engine* h) {
     CK(cudaMemcpyAsync(h->d_wsa, h->s_wsa, n * sizeof(uint32_t), cudaMemcpyDeviceToDevice, h->stream));
     CK(cudaMemcpyAsync(h->d_st, h->s_st, n * sizeof(uint2), cudaMemcpyDeviceToDevice, h->stream));
     CK(cudaMemcpyAsync(h->d_plane, h->s_plane, h->plane_bytes, cudaMemcpyDeviceToDevice, h->stream));
+    CK(cudaMemcpyAsync(h->d_danger, h->s_danger, h->plane_bytes, cudaMemcpyDeviceToDevice, h->stream));
     CK(cudaMemsetAsync(h->d_tgt, 0xFF, n * sizeof(uint32_t), h->stream));
     CK(cudaMemsetAsync(h->d_lost, 0xFF, n * sizeof(uint32_t), h->stream));
     CK(cudaMemsetAsync(h->d_claim, 0xFF, h->claim_cells * sizeof(uint32_t), h->stream));
@@ -1388,10 +1400,10 @@ extern "C" int epi_tick_hour_noalloc(const epi_params* params, uint32_t hour, ui
     } else {
         NOALLOC_CK(cudaMemsetAsync(d_claim, 0xFF, claim_bytes, s));
         const DecideKernel decide = decide_kernel(hod);
-        decide<<<blocks, kThreads, 0, s>>>(d_params, nullptr, n_chunks, pos, st, home, work, work_start_at, plane, d_claim,
-                                           d_tgt, nullptr, counts, d_hour, 0u, d_err);
-        k_commit<kCommitSlots><<<commit_blocks_for(n), kThreads, 0, s>>>(d_params, nullptr, n, pos, d_tgt, plane, d_claim, nullptr,
-                                                           d_hour, 0u);
+        decide<<<blocks, kThreads, 0, s>>>(d_params, nullptr, n_chunks, pos, st, home, work, work_start_at, plane, nullptr,
+                                           d_claim, d_tgt, nullptr, counts, d_hour, 0u, d_err);
+        k_commit<kCommitSlots><<<commit_blocks_for(n), kThreads, 0, s>>>(d_params, nullptr, n, pos, d_tgt, plane, nullptr,
+                                                                         d_claim, nullptr, d_hour, 0u);
     }
     NOALLOC_CK(cudaGetLastError());
     int err = 0;

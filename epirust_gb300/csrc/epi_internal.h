@@ -57,6 +57,7 @@ constexpr uint32_t kClaimWindow = 128;
 EPI_HD uint32_t claim_key(uint32_t hour, uint32_t agent) {
     return ((kClaimWindow - 1u - (hour & (kClaimWindow - 1u))) << kClaimAgentBits) | agent;
 }
+constexpr uint32_t kMaxGrid = 16382;          // coordinates fit 14 bits of a target word (never all ones)
 constexpr uint32_t kWorldHour = 0xFFFFFFFFu; // Philox counter word 1 of world-build draws
 constexpr uint32_t kMaxHours = 1500000u;     // infection day fits 16 bits
 

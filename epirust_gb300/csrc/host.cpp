@@ -114,7 +114,7 @@ std::string validate_params(const epi_params& p) {
     auto pct = [](double v) { return v >= 0.0 && v <= 1.0; };  // validate_percentage, custom_types.rs:29-35
     if (p.number_of_agents == 0) return "population is empty (No citizens!)";
     if (p.number_of_agents > kMaxAgentsPerWorld) return "number_of_agents must be <= 33554431 per world";
-    if (p.grid_size < 1 || p.grid_size > 32766) return "grid_size must be in [1, 32766]";
+    if (p.grid_size < 1 || p.grid_size > kMaxGrid) return "grid_size must be in [1, 16382]";
     if (p.hours > kMaxHours) return "hours must be <= 1500000 (16-bit infection day on the device)";
     if (!pct(p.public_transport_percentage) || !pct(p.working_percentage)) return "population percentages must be in [0, 1]";
     if (!pct(p.hospital_beds_percentage)) return "hospital_beds_percentage must be in [0, 1]";

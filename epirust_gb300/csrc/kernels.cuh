@@ -113,10 +113,11 @@ __global__ void __launch_bounds__(kThreads) k_decide(const DevParams* __restrict
                                                      uint32_t n_chunks, const uint32_t* __restrict__ pos,
                                                      uint2* __restrict__ st, const uint32_t* __restrict__ home,
                                                      const uint32_t* __restrict__ work, uint32_t* __restrict__ wsa,
-                                                     const uint8_t* __restrict__ plane, uint32_t* __restrict__ claim,
-                                                     uint32_t* __restrict__ tgt, uint32_t* __restrict__ lost,
-                                                     uint32_t* __restrict__ counts, const uint32_t* __restrict__ hour_base,
-                                                     uint32_t hour_offset, int* err) {
+                                                     const uint8_t* __restrict__ plane, const uint8_t* __restrict__ danger,
+                                                     uint32_t* __restrict__ claim, uint32_t* __restrict__ tgt,
+                                                     uint32_t* __restrict__ lost, uint32_t* __restrict__ counts,
+                                                     const uint32_t* __restrict__ hour_base, uint32_t hour_offset,
+                                                     int* err) {
     __shared__ uint32_t sh[8];
     __shared__ DevParams sP;
     const DevParams& P = sP;
@@ -132,7 +133,7 @@ __global__ void __launch_bounds__(kThreads) k_decide(const DevParams* __restrict
             hosp_known = false;
         }
         if (!P.active) continue;
-        const PlaneView pl{plane + P.plane_off, P.G, P.WP, err};
+        const PlaneView pl{plane + P.plane_off, P.G, P.WP, err, danger ? danger + P.plane_off : nullptr};
         uint32_t* rclaim = claim + P.claim_off;
         const uint32_t slot = c * kChunk + threadIdx.x;
         const uint32_t i = slot - P.agent_off;  // index within the replicate
@@ -197,8 +198,8 @@ __global__ void __launch_bounds__(kThreads) k_decide(const DevParams* __restrict
             // the plane byte changes when the agent moves or its class changes (s == s0 keeps it)
             uint32_t t = kNoAction;
             if (moving || s != s0) {
-                const uint32_t cls = cell_class(P, s);
-                if (moving || cls != cell_class(P, s0)) t = encode_target(nc, cls);
+                const uint32_t cls = cell_class(P, s), cls0 = cell_class(P, s0);
+                if (moving || cls != cls0) t = encode_target(nc, cls, cls0);
             }
             tgt[slot] = t;
             if (s != s0 || at != at0) st[slot] = make_uint2(s, at);
@@ -221,7 +222,7 @@ template <int S>
 __global__ void __launch_bounds__(kThreads) k_commit(const DevParams* __restrict__ Pall, const uint32_t* __restrict__ chunk_rep,
                                                      uint32_t n_slots, uint32_t* __restrict__ pos,
                                                      const uint32_t* __restrict__ tgt, uint8_t* __restrict__ plane,
-                                                     const uint32_t* __restrict__ claim,
+                                                     uint8_t* __restrict__ danger, const uint32_t* __restrict__ claim,
                                                      const uint32_t* __restrict__ lost,
                                                      const uint32_t* __restrict__ hour_base, uint32_t hour_offset) {
     const uint32_t hour = *hour_base + hour_offset;
@@ -256,14 +257,24 @@ __global__ void __launch_bounds__(kThreads) k_commit(const DevParams* __restrict
         const uint32_t i = slot - P.agent_off;
         const uint32_t WP = (uint32_t)P.WP;
         uint8_t* rplane = plane + P.plane_off;
-        const uint32_t xy = target_xy(t[k]), cls = target_class(t[k]);
+        const uint32_t xy = target_xy(t[k]), cls = target_class(t[k]), cls0 = target_old_class(t[k]);
         const size_t old_cell = (size_t)(unpack_y(p[k]) + 1) * WP + (unpack_x(p[k]) + 1);
+        size_t new_cell = old_cell;
         if (won[k] == claim_key(hour, i)) {
+            new_cell = (size_t)(unpack_y(xy) + 1) * WP + (unpack_x(xy) + 1);
             rplane[old_cell] = 0;
-            rplane[(size_t)(unpack_y(xy) + 1) * WP + (unpack_x(xy) + 1)] = (uint8_t)cls;
+            rplane[new_cell] = (uint8_t)cls;
             pos[slot] = xy;
         } else {
             rplane[old_cell] = (uint8_t)cls;
+        }
+        // infectious-neighbour counts follow infectious agents that move or stop or start
+        // being infectious (rare: a few agents per hour)
+        const bool inf0 = cls0 >= 2u, inf1 = cls >= 2u;
+        if (danger && (inf0 || inf1) && (inf0 != inf1 || new_cell != old_cell)) {
+            uint8_t* rd = danger + P.plane_off;
+            if (inf0) danger_add(rd, old_cell, WP, -1);
+            if (inf1) danger_add(rd, new_cell, WP, +1);
         }
     }
 }
@@ -271,14 +282,17 @@ __global__ void __launch_bounds__(kThreads) k_commit(const DevParams* __restrict
 // Plane bytes of every agent of every replicate (world upload).
 __global__ void k_build_plane(const DevParams* __restrict__ Pall, const uint32_t* __restrict__ chunk_rep, uint32_t n_slots,
                               const uint32_t* __restrict__ pos, const uint2* __restrict__ st, uint8_t* __restrict__ plane,
-                              int* err) {
+                              uint8_t* __restrict__ danger, int* err) {
     for (uint32_t slot = blockIdx.x * blockDim.x + threadIdx.x; slot < n_slots; slot += gridDim.x * blockDim.x) {
         const DevParams& P = Pall[chunk_rep ? chunk_rep[slot / kChunk] : 0u];
         if (slot - P.agent_off >= P.n) continue;
         const uint32_t p = pos[slot];
         const int32_t x = unpack_x(p), y = unpack_y(p);
         if (x > P.G || y > P.G) { atomicOr(err, 2); continue; }
-        plane[P.plane_off + (size_t)(y + 1) * P.WP + (x + 1)] = (uint8_t)cell_class(P, st[slot].x);
+        const size_t c = (size_t)(y + 1) * P.WP + (x + 1);
+        const uint32_t cls = cell_class(P, st[slot].x);
+        plane[P.plane_off + c] = (uint8_t)cls;
+        if (danger && cls >= 2u) danger_add(danger + P.plane_off, c, (uint32_t)P.WP, +1);
     }
 }
 
@@ -315,6 +329,27 @@ __global__ void k_check_agents(const DevParams* __restrict__ Pall, const uint32_
         if (x > P.G || y > P.G || plane[P.plane_off + (size_t)(y + 1) * P.WP + (x + 1)] != cell_class(P, st[slot].x))
             atomicAdd(bad, 1ull);
     }
+}
+
+// Cells of [0, G]^2 whose infectious-neighbour count differs from the 3x3 of the plane
+// (replicates r = blockIdx.y, blockIdx.y + gridDim.y, ...).
+__global__ void k_check_danger(const DevParams* __restrict__ Pall, uint32_t R, const uint8_t* __restrict__ plane,
+                               const uint8_t* __restrict__ danger, unsigned long long* bad) {
+    unsigned long long b = 0;
+    for (uint32_t r = blockIdx.y; r < R; r += gridDim.y) {
+        const DevParams& P = Pall[r];
+        const uint32_t side = (uint32_t)P.G + 1u, cells = side * side, WP = (uint32_t)P.WP;
+        const uint8_t* pl = plane + P.plane_off;
+        const uint8_t* dg = danger + P.plane_off;
+        for (uint32_t q = blockIdx.x * blockDim.x + threadIdx.x; q < cells; q += gridDim.x * blockDim.x) {
+            const size_t c = (size_t)(q / side + 1) * WP + (q % side + 1);
+            const uint32_t n = (pl[c - WP - 1] >= 2u) + (pl[c - WP] >= 2u) + (pl[c - WP + 1] >= 2u) +
+                               (pl[c - 1] >= 2u) + (pl[c + 1] >= 2u) + (pl[c + WP - 1] >= 2u) + (pl[c + WP] >= 2u) +
+                               (pl[c + WP + 1] >= 2u);
+            b += n != dg[c];
+        }
+    }
+    if (b) atomicAdd(bad, b);
 }
 
 // Occupied plane bytes over the whole buffer (borders and slack included: they must be 0).

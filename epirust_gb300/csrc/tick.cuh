@@ -29,6 +29,9 @@ struct PlaneView {
     const uint8_t* __restrict__ cells;  // padded plane: cell (x, y) at (y + 1) * WP + (x + 1)
     int32_t G, WP;
     int* err;
+    // Per cell, the number of infectious agents (class >= 2) on its 8 neighbours, same
+    // layout as cells; nullptr when the caller keeps none (the 3x3 is then read instead).
+    const uint8_t* __restrict__ danger;
     // Cells outside [0, G]^2 are never addressed by construction; if one were, it is
     // reported through err and treated as occupied instead of being dereferenced.
     __device__ __forceinline__ bool inside(int32_t x, int32_t y) const {
@@ -42,6 +45,13 @@ struct PlaneView {
         return __ldg(cells + (size_t)(y + 1) * (size_t)WP + (size_t)(x + 1));
     }
     __device__ __forceinline__ bool vacant(int32_t x, int32_t y) const { return at(x, y) == 0u; }
+    __device__ __forceinline__ uint32_t danger_at(int32_t x, int32_t y) const {
+        if (!inside(x, y)) {
+            atomicOr(err, 1);
+            return 0u;
+        }
+        return __ldg(danger + (size_t)(y + 1) * (size_t)WP + (size_t)(x + 1));
+    }
     // Bytes of (x-1, y), (x, y), (x+1, y) in bits 0-7, 8-15, 16-23.
     __device__ __forceinline__ uint32_t row3(int32_t x, int32_t y) const {
         const uintptr_t a = (uintptr_t)(cells + (size_t)(y + 1) * (size_t)WP + (size_t)x);
@@ -204,8 +214,10 @@ __device__ __forceinline__ void infection_dynamics(const DevParams& P, const Pla
     const uint32_t v = s & kStateMask;
     if (v == EPI_S) {
         if (s & (kWq | kVacc)) return;
+        // no infectious neighbour: no draw can succeed (the centre is vacant or the agent's own)
+        if (pl.danger && pl.danger_at(cell.x, cell.y) == 0u) return;
         const Rows3 rows = rows_around(pl, cell.x, cell.y);
-        if (!any_infectious(rows)) return;  // no infectious neighbour: no draw can succeed
+        if (!any_infectious(rows)) return;
         const uint32_t cand = valid_neighbours(cur, pl.G, cell.x, cell.y) & infectious_mask(rows);
         if (!cand) return;
         const uint32_t high = high_mask(rows);
@@ -403,11 +415,27 @@ __device__ __forceinline__ uint32_t count_bin(uint32_t s) {
     return (s & kHosp) ? 3u : 2u;
 }
 
-// tgt word: target x | y << 16 with the new plane class in bits 15 (low) and 31 (high).
-__device__ __forceinline__ uint32_t encode_target(Cell c, uint32_t cls) {
-    return pack_xy(c.x, c.y) | ((cls & 1u) << 15) | ((cls >> 1) << 31);
+// tgt word: target x | y << 16 (14 bits each, grids up to 16,383) with the new plane class
+// in bits 15 (low) and 31 (high) and the class before the hour in bits 14 and 30.
+__device__ __forceinline__ uint32_t encode_target(Cell c, uint32_t cls, uint32_t old_cls) {
+    return pack_xy(c.x, c.y) | ((cls & 1u) << 15) | ((cls >> 1) << 31) | ((old_cls & 1u) << 14) | ((old_cls >> 1) << 30);
 }
-__device__ __forceinline__ uint32_t target_xy(uint32_t t) { return t & 0x7FFF7FFFu; }
+__device__ __forceinline__ uint32_t target_xy(uint32_t t) { return t & 0x3FFF3FFFu; }
 __device__ __forceinline__ uint32_t target_class(uint32_t t) { return ((t >> 15) & 1u) | ((t >> 30) & 2u); }
+__device__ __forceinline__ uint32_t target_old_class(uint32_t t) { return ((t >> 14) & 1u) | ((t >> 29) & 2u); }
+
+// Add delta (+1 / -1) to the infectious-neighbour count of the 8 cells around the padded
+// plane index c (atomically, on the 32-bit words holding the bytes; counts stay in 0..8).
+__device__ __forceinline__ void danger_add(uint8_t* danger, size_t c, uint32_t WP, int delta) {
+    const size_t nb[8] = {c - WP - 1, c - WP, c - WP + 1, c - 1, c + 1, c + WP - 1, c + WP, c + WP + 1};
+#pragma unroll
+    for (int k = 0; k < 8; ++k) {
+        const uintptr_t a = (uintptr_t)(danger + nb[k]);
+        uint32_t* w = (uint32_t*)(a & ~(uintptr_t)3);
+        const uint32_t one = 1u << ((a & 3u) * 8u);
+        if (delta > 0) atomicAdd(w, one);
+        else atomicSub(w, one);
+    }
+}
 
 }  // namespace epi

@@ -226,7 +226,7 @@ static inline int o_world_init(o_world* w, const epi_params* p) {
     w->W = w->G + 1;
     w->key[0] = (uint32_t)p->seed;
     w->key[1] = (uint32_t)(p->seed >> 32);
-    if (p->grid_size < 1 || p->grid_size > 32766 || p->number_of_agents == 0) return EPI_ERR_CONFIG;
+    if (p->grid_size < 1 || p->grid_size > 16382 || p->number_of_agents == 0) return EPI_ERR_CONFIG;
     o_define_geography(w);
     return EPI_OK;
 }
