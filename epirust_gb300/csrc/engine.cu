@@ -140,6 +140,9 @@ static DevParams make_dev_params(const epi_params& p, const epi_geography& geo0,
     d.area[kHosp1] = to_rect(grown_hospital(geo0));
     d.key0 = (uint32_t)p.seed;
     d.key1 = (uint32_t)(p.seed >> 32);
+    uint32_t mk[4];
+    philox4x32(0u, kWorldHour, kBlkMoveKey, 0u, d.key0, d.key1, mk);
+    d.move_key = mk[0];
     d.reg_start = p.regular_transmission_start_day;
     d.high_start = p.high_transmission_start_day;
     d.last_day = p.last_day;

@@ -90,6 +90,7 @@ struct DevParams {
     uint32_t hosp_code;         // kHosp0 or kHosp1: the current hospital_area
     Rect area[kNumAreas];       // global areas by code (HOME/WORK slots unused)
     uint32_t key0, key1;        // Philox key = seed
+    uint32_t move_key;          // key of the Philox2x32 movement draws
     uint32_t reg_start, high_start, last_day;
     uint32_t exposed_duration, pre_duration;
     uint32_t hosp_if_class;     // bit c: rate of class c >= high rate (c = 0 none, 1 reg, 2 high)
@@ -143,16 +144,38 @@ EPI_HD void philox4x32(uint32_t c0, uint32_t c1, uint32_t c2, uint32_t c3, uint3
     out[0] = c0; out[1] = c1; out[2] = c2; out[3] = c3;
 }
 
-// Draw-block ids of the counter word 2 (the layout every consumer of the streams shares).
+// Philox2x32-10 (same paper): (R0, R1) -> (hi(M R0) ^ key ^ R1, lo(M R0)), key += Weyl.
+EPI_HD void philox2x32(uint32_t c0, uint32_t c1, uint32_t key, uint32_t out[2]) {
+    for (int r = 0; r < 10; ++r) {
+#if defined(__CUDA_ARCH__)
+        const uint32_t hi = __umulhi(0xD256D193u, c0), lo = 0xD256D193u * c0;
+#else
+        const uint64_t pr = 0xD256D193ull * c0;
+        const uint32_t hi = (uint32_t)(pr >> 32), lo = (uint32_t)pr;
+#endif
+        c0 = hi ^ key ^ c1;
+        c1 = lo;
+        key += 0x9E3779B9u;
+    }
+    out[0] = c0;
+    out[1] = c1;
+}
+
+// Movement draws: Philox2x32-10 keyed by DevParams::move_key (word 0 of the Philox4x32
+// block (0, kWorldHour, kBlkMoveKey, 0) of the seed), counter (agent | which, hour):
+constexpr uint32_t kMoveChoice = 0u;        // word 0: Moore choice (movement) / death (hour 23)
+constexpr uint32_t kMovePoint = 1u << 25;   // words 0,1: random point x, y
+
+// Draw-block ids of the Philox4x32 counter word 2 (the layout every consumer shares).
 enum DrawBlock : uint32_t {
-    kBlkMove = 0,     // u0,u1 random point; u2 Moore choice (movement) / death (hour 23)
     kBlkDisease = 1,  // Susceptible neighbours 0-3 | Exposed jitter, symptoms | Pre severe
     kBlkDisease2 = 2, // Susceptible neighbours 4-7
     kBlkVaccine = 3,
     kBlkCitizen = 16, // world build: working, public transport, hospital staff, immunity
     kBlkEssential = 17,
     kBlkHouse = 18,   // counter word 0 = house index
-    kBlkInfectPick = 19
+    kBlkInfectPick = 19,
+    kBlkMoveKey = 20  // counter word 2 of the movement key's block
 };
 
 }  // namespace epi

@@ -157,7 +157,7 @@ __global__ void __launch_bounds__(kThreads) k_decide(const DevParams* __restrict
             const uint32_t s0 = s, at0 = at;
             const uint32_t hm = home[slot], wk = work[slot];
             const Cell cell{unpack_x(p), unpack_y(p)};
-            Draws dr{i, hour, P.key0, P.key1};
+            Draws dr{i, hour, P.key0, P.key1, P.move_key};
             Cell nc;
             bool infect = false;
             if (HC == kHcStart) {

@@ -121,14 +121,19 @@ __device__ __forceinline__ int nth_set_bit8(uint32_t m, uint32_t j) {
     return base;
 }
 
-// Lazily materialised Philox blocks of one agent-hour.
+// Lazily materialised Philox blocks of one agent-hour: m(0), m(1) the random-point words
+// and m(2) the choice word (Philox2x32 each), d(), d2() the disease blocks (Philox4x32).
 struct Draws {
-    uint32_t agent, hour, k0, k1;
+    uint32_t agent, hour, k0, k1, mk;
     uint32_t have = 0;
-    uint32_t b0[4], b1[4], b2[4];
+    uint32_t pt[2], ch[2], b1[4], b2[4];
     __device__ __forceinline__ uint32_t m(int w) {
-        if (!(have & 1u)) { philox4x32(agent, hour, kBlkMove, 0u, k0, k1, b0); have |= 1u; }
-        return b0[w];
+        if (w < 2) {
+            if (!(have & 1u)) { philox2x32(agent | kMovePoint, hour, mk, pt); have |= 1u; }
+            return pt[w];
+        }
+        if (!(have & 8u)) { philox2x32(agent | kMoveChoice, hour, mk, ch); have |= 8u; }
+        return ch[0];
     }
     __device__ __forceinline__ uint32_t d(int w) {
         if (!(have & 2u)) { philox4x32(agent, hour, kBlkDisease, 0u, k0, k1, b1); have |= 2u; }
@@ -321,15 +326,6 @@ __device__ __forceinline__ Cell perform_movements(const DevParams& P, const Plan
     } else {
         const Rect cur = area_rect(P, st_area(s), home, work);
         const bool worker = ws != EPI_WS_NA;  // Normal or Essential here
-        if (HC != kHcMove) {
-            // Both work-status arms below draw from the movement block whenever the agent
-            // moves at all; materialising it here, before the branch, runs the Philox rounds
-            // once per warp instead of once per arm.  (Draws are pure functions of the
-            // counter: an unused block changes nothing.)
-            const uint32_t v = s & kStateMask;
-            const bool override_home = HC == kHcHome && worker && (v == EPI_I_MILD || v == EPI_I_SEVERE);
-            if (can_move(s) || override_home) (void)dr.m(0);
-        }
         if (HC == kHcMove) {
             nc = move_agent_from(pl, s, cur, cell, dr);
         } else if (HC == kHcTransport) {

@@ -396,6 +396,7 @@ void o1_geography_increase_hospital_size(epi_geography* g, uint32_t grid_size) {
     g->hospital.y1 = (int32_t)grid_size;
 }
 void o1_philox(const uint32_t ctr[4], const uint32_t key[2], uint32_t out[4]) { orc_philox4x32_10(ctr, key, out); }
+void o1_philox2x32(const uint32_t ctr[2], uint32_t key, uint32_t out[2]) { orc_philox2x32_10(ctr, key, out); }
 /* Area::get_neighbors_of, area.rs:147-149 */
 void o1_area_neighbors(int32_t x0, int32_t y0, int32_t x1, int32_t y1, int32_t px, int32_t py, int32_t* out, uint32_t* n) {
     area a = mk_area(x0, y0, x1, y1);

@@ -7,9 +7,13 @@
  *
  * Randomness.  The reference draws from an unseeded thread_rng
  * (common/src/utils/random_wrapper.rs:27-30).  Here every draw is a fixed word of a
- * Philox4x32-10 block keyed by the world key, counter = (agent, hour, block, 0):
- *   block 0  movement / hour-0 / hour-23: u0,u1 = random point x,y; u2 = Moore choice
- *            (move_agent_from) or death draw (hour 23)
+ * counter-based Philox block.  The movement words come from Philox2x32-10 keyed by the
+ * world's movement key (word 0 of the Philox4x32-10 block (0, 0xFFFFFFFF, 20, 0) of the
+ * world key):
+ *   point    counter = (agent | 1 << 25, hour): u0,u1 = random point x,y
+ *   choice   counter = (agent, hour): u2 = Moore choice (move_agent_from) or death draw
+ *            (hour 23)
+ * The rest come from Philox4x32-10 keyed by the world key, counter = (agent, hour, block, 0):
  *   block 1  disease: Susceptible neighbours 0-3; Exposed u0 = jitter, u1 = symptoms;
  *            Pre u0 = severe
  *   block 2  Susceptible neighbours 4-7
@@ -56,6 +60,7 @@ typedef struct {
     area housing, transport, work_area, hospital;
     uint32_t hfx, hfy, ofx, ofy;
     uint32_t key[2];
+    uint32_t move_key;      /* key of the Philox2x32 movement draws */
 } o_world;
 
 static inline void draw4(const o_world* w, uint32_t c0, uint32_t c1, uint32_t c2, uint32_t out[4]) {
@@ -118,13 +123,34 @@ static inline int can_move(const citizen* c) {
 }
 static inline int is_working(const citizen* c) { return c->ws != EPI_WS_NA; }
 
-/* lazily materialised Philox blocks of one agent-hour */
-typedef struct { const o_world* w; uint32_t agent, hour; int have[3]; uint32_t blk[3][4]; } draws;
+/* lazily materialised Philox blocks of one agent-hour; "block 0" words 0,1 are the point
+   draw and word 2 the choice draw (Philox2x32), blocks 1, 2 are Philox4x32 */
+typedef struct { const o_world* w; uint32_t agent, hour; int have[3], have_point, have_choice; uint32_t blk[3][4];
+                 uint32_t point[2], choice; } draws;
 static inline void draws_init(draws* d, const o_world* w, uint32_t agent, uint32_t hour) {
     d->w = w; d->agent = agent; d->hour = hour;
     d->have[0] = d->have[1] = d->have[2] = 0;
+    d->have_point = d->have_choice = 0;
 }
 static inline uint32_t dr(draws* d, int b, int k) {
+    if (b == 0) {
+        if (k < 2) {
+            if (!d->have_point) {
+                const uint32_t ctr[2] = {d->agent | (1u << 25), d->hour};
+                orc_philox2x32_10(ctr, d->w->move_key, d->point);
+                d->have_point = 1;
+            }
+            return d->point[k];
+        }
+        if (!d->have_choice) {
+            const uint32_t ctr[2] = {d->agent, d->hour};
+            uint32_t out[2];
+            orc_philox2x32_10(ctr, d->w->move_key, out);
+            d->choice = out[0];
+            d->have_choice = 1;
+        }
+        return d->choice;
+    }
     if (!d->have[b]) { draw4(d->w, d->agent, d->hour, (uint32_t)b, d->blk[b]); d->have[b] = 1; }
     return d->blk[b][k];
 }
@@ -226,6 +252,11 @@ static inline int o_world_init(o_world* w, const epi_params* p) {
     w->W = w->G + 1;
     w->key[0] = (uint32_t)p->seed;
     w->key[1] = (uint32_t)(p->seed >> 32);
+    {
+        uint32_t mk[4];
+        draw4(w, 0u, WB_HOUR, 20u, mk);
+        w->move_key = mk[0];
+    }
     if (p->grid_size < 1 || p->grid_size > 16382 || p->number_of_agents == 0) return EPI_ERR_CONFIG;
     o_define_geography(w);
     return EPI_OK;

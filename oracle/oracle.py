@@ -154,6 +154,7 @@ def lib():
     L.o1_resize_hospital.argtypes = [P(Geography), C.c_int32, C.c_double, C.c_double]
     L.o1_geography_increase_hospital_size.argtypes = [P(Geography), C.c_uint32]
     L.o1_philox.argtypes = [P(C.c_uint32), P(C.c_uint32), P(C.c_uint32)]
+    L.o1_philox2x32.argtypes = [P(C.c_uint32), C.c_uint32, P(C.c_uint32)]
     L.o1_area_neighbors.argtypes = [C.c_int32] * 6 + [P(C.c_int32), P(C.c_uint32)]
     L.o1_area_cells.restype = C.c_uint32
     L.o1_area_cells.argtypes = [C.c_int32] * 4 + [P(C.c_int32), C.c_uint32]
@@ -306,6 +307,13 @@ def philox(ctr, key) -> list[int]:
     k = (C.c_uint32 * 2)(*key)
     o = (C.c_uint32 * 4)()
     lib().o1_philox(c, k, o)
+    return list(o)
+
+
+def philox2x32(ctr, key: int) -> list[int]:
+    c = (C.c_uint32 * 2)(*ctr)
+    o = (C.c_uint32 * 2)()
+    lib().o1_philox2x32(c, key, o)
     return list(o)
 
 

@@ -13,6 +13,13 @@ from helpers import SMALL_POX, golden, hospital_world, make_config
 S, E, I_PRE, I_ASYM, I_MILD, I_SEVERE, R, D = range(8)
 
 
+def test_philox2x32_known_answers(oracle_mod):
+    # Salmon et al. SC'11 / Random123 kat_vectors, philox2x32 with 10 rounds
+    assert oracle_mod.philox2x32([0, 0], 0) == [0xFF1DAE59, 0x6CD10DF2]
+    assert oracle_mod.philox2x32([0xFFFFFFFF, 0xFFFFFFFF], 0xFFFFFFFF) == [0x2C3F628B, 0xAB4FD7AD]
+    assert oracle_mod.philox2x32([0x243F6A88, 0x85A308D3], 0x13198A2E) == [0xDD7CE038, 0xF62A4C12]
+
+
 def test_philox_known_answers(oracle_mod):
     # Salmon et al. SC'11 / Random123 kat_vectors, philox4x32 with 10 rounds
     assert oracle_mod.philox([0, 0, 0, 0], [0, 0]) == [0x6627E8D5, 0xE169C58D, 0xBC57AC4C, 0x9B00DBD8]
