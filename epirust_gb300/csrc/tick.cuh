@@ -6,14 +6,17 @@
 // The rules follow engine/src/citizen/mod.rs:215-454,
 // engine/src/state_machine/default_disease_handler.rs:31-103 and
 // engine/src/allocation_map.rs:136-163; random draws are fixed words of per-agent-hour
-// Philox blocks (counter = agent, hour, block, 0).
+// Philox blocks (movement: Philox2x32, counter = agent | which, hour; disease: Philox4x32,
+// counter = agent, hour, block, 0).
 //
 // Moore neighbourhoods are evaluated as bit masks: the byte plane carries a one-cell border,
 // so the 3x3 block around any cell of [0, G]^2 is in bounds; each of its three rows comes in
 // as two aligned 32-bit loads and a funnel shift, and SWAR tests turn the nine bytes into
 // 8-bit masks (bit k = k-th neighbour in NeighborIterator order) of occupied, infectious and
 // high-rate neighbours.  The area and grid filters of get_neighbors_of / is_point_in_grid
-// become a second mask built from six comparisons.
+// become a second mask built from six comparisons.  A per-cell count of infectious
+// neighbours (maintained by k_commit) lets a susceptible agent skip the exposure block when
+// it is zero.
 #pragma once
 
 #include "epi_internal.h"
