@@ -380,6 +380,18 @@ def run_gpu(args, cfg):
     alg_bytes = DECIDE_BYTES_PER_AGENT * n + cells
     achieved = alg_bytes / (avg_ms / 1000.0) / 1e9
     peak, peak_kind = _peaks()
+    # issue roofline: warp instructions per k_decide launch (committed ncu launch list, scaled
+    # by agents) over the launch time, against 4 schedulers x SMs x the maximum SM clock
+    issue = None
+    ipath = os.path.join(ROOT, "profiles", "k_decide_issue.txt")
+    if os.path.exists(ipath):
+        with open(ipath) as f:
+            inst = int(f.readline().rsplit(":", 1)[1]) * n / 1_000_000
+        sms = torch.cuda.get_device_properties(dev_index).multi_processor_count
+        mhz = clocks.get("sm_max_mhz") or 2070.0
+        peak_issue = 4.0 * sms * mhz * 1e6
+        issue = {"achieved": inst / (avg_ms / 1000.0), "peak": peak_issue, "unit": "warp-instructions/s",
+                 "frac": inst / (avg_ms / 1000.0) / peak_issue, "inst_per_launch": inst}
     traffic = None  # DRAM bytes of one k_decide launch from the committed ncu capture
     tpath = os.path.join(ROOT, "profiles", "k_decide_traffic.txt")
     if os.path.exists(tpath):
@@ -407,6 +419,7 @@ def run_gpu(args, cfg):
                          "frac": achieved / peak, "peak_kind": peak_kind, "traffic": traffic,
                          "alg_bytes_per_launch": alg_bytes, "avg_launch_ms": avg_ms,
                          "share_of_kernel_time": ms_d / total_kernel_ms if total_kernel_ms else None,
+                         "issue": issue,
                          "kernels": {k: {"launches": v[0], "ms": v[1]} for k, v in stats.items() if v[0]}},
             "cpu_baseline": cpu,
             "e2e": {"value": e2e_value, "unit": METRIC, "h2d_bytes_per_step": int(n * 24),

@@ -105,7 +105,7 @@ EXPORTS = [
     "epi_ensemble_replicates", "epi_ensemble_run", "epi_ensemble_snapshot", "epi_ensemble_check",
     "epi_ensemble_save_state", "epi_ensemble_restore_state", "epi_ensemble_set_profiling", "epi_ensemble_kernel_stats",
     "epi_ensemble_kernels_launched", "epi_ensemble_hour_bytes", "epi_engine_autotune", "epi_engine_set_launch_shape",
-    "epi_engine_launch_shape", "epi_ensemble_autotune",
+    "epi_engine_launch_shape", "epi_ensemble_autotune", "epi_engine_state_stream_open", "epi_engine_state_stream_close",
 ]
 
 
@@ -205,6 +205,8 @@ def lib():
     _sig(L, "epi_engine_set_launch_shape", C.c_int, [V, P(LaunchShape)])
     _sig(L, "epi_engine_launch_shape", C.c_int, [V, P(LaunchShape)])
     _sig(L, "epi_ensemble_autotune", C.c_int, [V, C.c_uint32, P(LaunchShape)])
+    _sig(L, "epi_engine_state_stream_open", C.c_int, [V, C.c_char_p])
+    _sig(L, "epi_engine_state_stream_close", C.c_int, [V])
     F = P(C.c_float)
     _sig(L, "epi_mlp_create", C.c_int, [P(MlpConfig), P(V)])
     _sig(L, "epi_mlp_destroy", C.c_int, [V])

@@ -5,6 +5,7 @@
 // --threads is accepted for compatibility; the tick runs on the GPU.
 #include <chrono>
 #include <cstdio>
+#include <cstdlib>
 #include <cstring>
 #include <fstream>
 #include <sstream>
@@ -12,6 +13,7 @@
 #include <vector>
 
 #include "../../include/epi_engine.h"
+#include "json.hpp"
 
 static void usage() {
     std::fprintf(stderr,
@@ -53,15 +55,35 @@ int main(int argc, char** argv) {
         return 1;
     }
     if (have_seed) p.seed = seed;
+    // enable_citizen_state_messages (common/src/config/mod.rs:55): the per-hour citizen states
+    // go to <output_dir>/output/citizen_states_0.bin (the reference publishes them to Kafka)
+    bool citizen_states = false;
+    try {
+        const epi::json::Value root = epi::json::parse(ss.str());
+        if (const epi::json::Value* v = root.get("enable_citizen_state_messages"))
+            citizen_states = v->kind == epi::json::Value::Bool && v->b;
+    } catch (const std::exception&) {
+    }
     auto t0 = std::chrono::steady_clock::now();
     epi_engine* h = nullptr;
     int rc = epi_engine_create(&p, &h);
     if (rc != EPI_OK) { std::fprintf(stderr, "engine create failed (%d): %s\n", rc, epi_engine_last_error(nullptr)); return 1; }
+    if (citizen_states) {
+        const std::string dir = out_dir + "/output";
+        std::string mk = "mkdir -p '" + dir + "'";
+        if (std::system(mk.c_str()) != 0 ||
+            epi_engine_state_stream_open(h, (dir + "/citizen_states_0.bin").c_str()) != EPI_OK) {
+            std::fprintf(stderr, "citizen-state stream: %s\n", epi_engine_last_error(h));
+            epi_engine_destroy(h);
+            return 1;
+        }
+    }
     auto t1 = std::chrono::steady_clock::now();
     std::vector<epi_counts> rows(p.hours ? p.hours : 1);
     uint32_t n_rows = 0;
     rc = epi_engine_run(h, rows.data(), (uint32_t)rows.size(), &n_rows);
     auto t2 = std::chrono::steady_clock::now();
+    if (rc == EPI_OK) rc = epi_engine_state_stream_close(h);
     if (rc != EPI_OK) { std::fprintf(stderr, "run failed (%d): %s\n", rc, epi_engine_last_error(h)); epi_engine_destroy(h); return 1; }
     // the standalone engine id is "0" (engine/src/engine_app.rs:30, 100-101)
     rc = epi_engine_write_outputs(h, out_dir.c_str(), "0");

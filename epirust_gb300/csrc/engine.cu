@@ -88,7 +88,7 @@ struct epi_engine {
         cudaGraphExec_t exec = nullptr;
         std::vector<TimedLaunch> events;
     };
-    std::map<std::tuple<uint32_t, uint32_t, bool>, HourGraph> graphs;
+    std::map<std::tuple<uint32_t, uint32_t, uint32_t>, HourGraph> graphs;
     std::string err;
     bool profiling = false;
     uint32_t launches[kKindCount] = {};
@@ -98,6 +98,16 @@ struct epi_engine {
     std::vector<TimedLaunch>* capture = nullptr;  // set while a profiling graph is captured
     uint64_t kernels_launched = 0;
     int64_t last_claim_hour = -1;  // latest hour whose claims may sit in the claim plane (-1: clean)
+    bool stop_rule = false;        // inside the run loop: hours after a replicate's stop do nothing
+    // citizen-state stream (single world): per-hour codes written by k_state_delta
+    FILE* stream_file = nullptr;
+    uint32_t* d_prev = nullptr;     // cell of every agent at the previous record
+    uint8_t* d_codes = nullptr;     // kStreamChunk x slots
+    uint2* d_exc = nullptr;         // kStreamChunk x slots (worst case: everyone jumps)
+    uint32_t* d_exc_n = nullptr;    // kStreamChunk
+    uint8_t* h_codes = nullptr;     // pinned mirrors
+    uint2* h_exc = nullptr;
+    uint32_t* h_exc_n = nullptr;
     // device-side checkpoint
     uint32_t *s_pos = nullptr, *s_wsa = nullptr;
     uint2* s_st = nullptr;
@@ -266,7 +276,7 @@ static int ensure_counts(epi_engine* h, uint32_t hours_needed) {
 // ------------------------------------------------------------------ the hour loop
 using DecideKernel = void (*)(const DevParams*, const uint32_t*, uint32_t, const uint32_t*, uint2*, const uint32_t*,
                               const uint32_t*, uint32_t*, const uint8_t*, const uint8_t*, uint32_t*, uint32_t*, uint32_t*,
-                              uint32_t*, const uint32_t*, uint32_t, int*);
+                              uint32_t*, const uint32_t*, uint32_t, int*, const uint32_t*);
 
 // Hours 2..6 of a day change nothing once hour 1 has sent everyone but hospital staff home
 // (routine, citizen/mod.rs:243-247, sets current_area = home_location and nothing else), so
@@ -297,7 +307,7 @@ static int commit_blocks_for(uint32_t slots, int per_thread = kCommitSlots) {
 
 // k_commit with S slots per thread.
 using CommitKernel = void (*)(const DevParams*, const uint32_t*, uint32_t, uint32_t*, const uint32_t*, uint8_t*,
-                              uint8_t*, const uint32_t*, const uint32_t*, const uint32_t*, uint32_t);
+                              uint8_t*, const uint32_t*, const uint32_t*, const uint32_t*, uint32_t, const uint32_t*);
 static CommitKernel commit_kernel(int slots_per_thread) {
     switch (slots_per_thread) {
         case 1: return k_commit<1>;
@@ -316,27 +326,47 @@ static uint32_t window_start_offset(uint32_t first_hour, uint32_t nh) {
 static int enqueue_hours(epi_engine* h, uint32_t first_hour, uint32_t nh) {
     const size_t row_words = (size_t)h->R() * 8;
     CK(cudaMemsetAsync(h->d_counts, 0, (size_t)nh * row_words * sizeof(uint32_t), h->stream));
+    if (h->stream_file) CK(cudaMemsetAsync(h->d_exc_n, 0, (size_t)nh * sizeof(uint32_t), h->stream));
     const uint32_t n_chunks = h->slots / kChunk;
+    int last_row = -1;  // the latest hour of the segment whose counts the kernels computed
     for (uint32_t k = 0; k < nh; ++k) {
         const uint32_t hod = (first_hour + k) % 24u;
         uint32_t* rows = h->d_counts + (size_t)k * row_words;
+        const uint32_t* prev = h->stop_rule && last_row >= 0 ? h->d_counts + (size_t)last_row * row_words : nullptr;
         if (k > 0 && (first_hour + k) % kClaimWindow == 0) CK(cudaMemsetAsync(h->d_claim, 0xFF, h->claim_cells * sizeof(uint32_t), h->stream));
+        if (h->stream_file) {  // record the previous hour's end state before this hour changes it
+            if (k > 0) {
+                const uint32_t n = h->reps[0].n;
+                k_state_delta<<<(n + kThreads - 1) / kThreads, kThreads, 0, h->stream>>>(
+                    n, h->d_pos, h->d_st, h->d_prev, h->d_codes + (size_t)(k - 1) * h->slots,
+                    h->d_exc + (size_t)(k - 1) * h->slots, h->d_exc_n + (k - 1));
+                CK(cudaGetLastError());
+            }
+        }
         if (sleep_hour_skipped(first_hour, k)) continue;
+        last_row = (int)k;
         if (hod >= 1u && hod <= 6u) {
             LAUNCH(kKSleep, (k_sleep<<<h->grid_blocks, kThreads, 0, h->stream>>>(h->d_params, h->d_chunk_rep, n_chunks,
-                                                                                  h->d_st, rows)));
+                                                                                  h->d_st, rows, prev)));
         } else {
             const DecideKernel decide = decide_kernel(hod);
             LAUNCH(kKDecide, (decide<<<h->grid_blocks, kThreads, 0, h->stream>>>(
                                   h->d_params, h->d_chunk_rep, n_chunks, h->d_pos, h->d_st, h->d_home, h->d_work, h->d_wsa,
                                   h->d_plane, h->d_danger, h->d_claim, h->d_tgt, h->d_lost, rows, h->d_hour_base, k,
-                                  h->d_err)));
+                                  h->d_err, prev)));
             const CommitKernel commit = commit_kernel(h->commit_slots);
             LAUNCH(kKCommit, (commit<<<h->commit_blocks, kThreads, 0, h->stream>>>(h->d_params, h->d_chunk_rep, h->slots,
                                                                                    h->d_pos, h->d_tgt, h->d_plane, h->d_danger,
                                                                                    h->d_claim, h->d_lost, h->d_hour_base,
-                                                                                   k)));
+                                                                                   k, prev)));
         }
+    }
+    if (h->stream_file) {
+        const uint32_t n = h->reps[0].n;
+        k_state_delta<<<(n + kThreads - 1) / kThreads, kThreads, 0, h->stream>>>(
+            n, h->d_pos, h->d_st, h->d_prev, h->d_codes + (size_t)(nh - 1) * h->slots, h->d_exc + (size_t)(nh - 1) * h->slots,
+            h->d_exc_n + (nh - 1));
+        CK(cudaGetLastError());
     }
     CK(cudaMemcpyAsync(h->h_counts, h->d_counts, (size_t)nh * row_words * sizeof(uint32_t), cudaMemcpyDeviceToHost,
                        h->stream));
@@ -356,7 +386,7 @@ static int check_error_flag(epi_engine* h) {
 
 // Simulate hours first_hour .. first_hour + nh - 1 for every active replicate; the counts
 // of hour k of replicate r land in h_counts[(k * R + r) * 8 ..].
-static int run_hours(epi_engine* h, uint32_t first_hour, uint32_t nh) {
+static int run_hours_chunk(epi_engine* h, uint32_t first_hour, uint32_t nh) {
     if (nh == 0) return EPI_OK;
     if ((uint64_t)first_hour + nh > 0xFFFFFFFFull) { h->err = "hour out of range"; return EPI_ERR_ARG; }
     int rc = ensure_counts(h, nh);
@@ -372,7 +402,8 @@ static int run_hours(epi_engine* h, uint32_t first_hour, uint32_t nh) {
     CK(cudaMemcpyAsync(h->d_hour_base, h->h_hour_base, sizeof(uint32_t), cudaMemcpyHostToDevice, h->stream));
     {
         // the kernel sequence depends on the hours of the day and on where a claim window opens
-        auto key = std::make_tuple(first_hour % 24u + 24u * window_start_offset(first_hour, nh), nh, h->profiling);
+        auto key = std::make_tuple(first_hour % 24u + 24u * window_start_offset(first_hour, nh), nh,
+                                   (h->profiling ? 1u : 0u) | (h->stream_file ? 2u : 0u) | (h->stop_rule ? 4u : 0u));
         auto it = h->graphs.find(key);
         if (it == h->graphs.end()) {
             epi_engine::HourGraph hg;
@@ -411,10 +442,12 @@ static int run_hours(epi_engine* h, uint32_t first_hour, uint32_t nh) {
     if (rc) return rc;
     rc = check_error_flag(h);
     if (rc) return rc;
+    std::vector<uint8_t> ended(h->R(), 0);  // stop rule met at an earlier hour of this segment
     for (uint32_t k = 0; k < nh; ++k) {
         for (uint32_t r = 0; r < h->R(); ++r) {
-            if (!h->reps[r].active) continue;
+            if (!h->reps[r].active || ended[r]) continue;
             const uint32_t* c = h->h_counts + ((size_t)k * h->R() + r) * 8;
+            if (h->stop_rule && c[1] == 0 && c[2] == 0 && c[3] == 0) ended[r] = 1;
             const uint64_t total = (uint64_t)c[0] + c[1] + c[2] + c[3] + c[4] + c[5];
             if (total != h->reps[r].n) {  // assert_eq!(csv_record.total(), current_population), allocation_map.rs:128
                 h->err = "replicate " + std::to_string(r) + ": counts total " + std::to_string(total) + " != population " +
@@ -424,6 +457,74 @@ static int run_hours(epi_engine* h, uint32_t first_hour, uint32_t nh) {
         }
     }
     return EPI_OK;
+}
+
+// ------------------------------------------------------------------ citizen-state stream
+constexpr uint32_t kStreamChunk = 24;  // hours per stream buffer fill
+
+// Append hours first_hour .. first_hour + m - 1 of the stream buffers to the file: per hour
+// {hour, agents, exceptions} (u32 each), the agents' code bytes, then the exceptions
+// {agent, x | y << 16} in agent order.
+static int stream_write(epi_engine* h, uint32_t first_hour, uint32_t m) {
+    const uint32_t n = h->reps[0].n;
+    CK(cudaMemcpyAsync(h->h_exc_n, h->d_exc_n, m * sizeof(uint32_t), cudaMemcpyDeviceToHost, h->stream));
+    for (uint32_t k = 0; k < m; ++k)
+        CK(cudaMemcpyAsync(h->h_codes + (size_t)k * h->slots, h->d_codes + (size_t)k * h->slots, n,
+                           cudaMemcpyDeviceToHost, h->stream));
+    CK(cudaStreamSynchronize(h->stream));
+    for (uint32_t k = 0; k < m; ++k) {
+        const uint32_t ne = std::min(h->h_exc_n[k], n);
+        if (ne) CK(cudaMemcpy(h->h_exc, h->d_exc + (size_t)k * h->slots, ne * sizeof(uint2), cudaMemcpyDeviceToHost));
+        std::sort(h->h_exc, h->h_exc + ne, [](const uint2& a, const uint2& b) { return a.x < b.x; });
+        const uint32_t head[3] = {first_hour + k, n, ne};
+        if (std::fwrite(head, sizeof head, 1, h->stream_file) != 1 ||
+            std::fwrite(h->h_codes + (size_t)k * h->slots, 1, n, h->stream_file) != n ||
+            (ne && std::fwrite(h->h_exc, sizeof(uint2), ne, h->stream_file) != ne)) {
+            h->err = "citizen-state stream: write failed";
+            return EPI_ERR_IO;
+        }
+    }
+    return EPI_OK;
+}
+
+// Hours first_hour .. first_hour + nh - 1 (see run_hours_chunk); with the stream open they run
+// in chunks of at most kStreamChunk hours, each written out before the next.
+static int run_hours(epi_engine* h, uint32_t first_hour, uint32_t nh) {
+    if (!h->stream_file) return run_hours_chunk(h, first_hour, nh);
+    int rc = ensure_counts(h, std::max(nh, kStreamChunk));
+    if (rc) return rc;
+    const size_t row = (size_t)h->R() * 8;
+    std::vector<uint32_t> all((size_t)nh * row, 0u);
+    for (uint32_t k0 = 0; k0 < nh; k0 += kStreamChunk) {
+        const uint32_t m = std::min(kStreamChunk, nh - k0);
+        rc = run_hours_chunk(h, first_hour + k0, m);
+        if (rc) return rc;
+        // in the run loop the record ends with the hour the stop rule fires (the reference
+        // publishes no later hour)
+        uint32_t keep = m;
+        if (h->stop_rule)
+            for (uint32_t k = 0; k < m; ++k) {
+                const uint32_t* c = h->h_counts + (size_t)k * row;
+                if ((c[1] | c[2] | c[3]) == 0u) { keep = k + 1; break; }
+            }
+        rc = stream_write(h, first_hour + k0, keep);
+        if (rc) return rc;
+        std::memcpy(all.data() + (size_t)k0 * row, h->h_counts, (size_t)keep * row * sizeof(uint32_t));
+        if (keep < m) break;
+    }
+    std::memcpy(h->h_counts, all.data(), all.size() * sizeof(uint32_t));
+    return EPI_OK;
+}
+
+static void stream_free(epi_engine* h) {
+    if (h->stream_file) std::fclose(h->stream_file);
+    h->stream_file = nullptr;
+    cudaFree(h->d_prev); cudaFree(h->d_codes); cudaFree(h->d_exc); cudaFree(h->d_exc_n);
+    if (h->h_codes) cudaFreeHost(h->h_codes);
+    if (h->h_exc) cudaFreeHost(h->h_exc);
+    if (h->h_exc_n) cudaFreeHost(h->h_exc_n);
+    h->d_prev = nullptr; h->d_codes = nullptr; h->d_exc = nullptr; h->d_exc_n = nullptr;
+    h->h_codes = nullptr; h->h_exc = nullptr; h->h_exc_n = nullptr;
 }
 
 static epi_counts counts_of(const epi_engine* h, uint32_t k, uint32_t r, uint32_t hour) {
@@ -502,7 +603,9 @@ static int run_loop_body(epi_engine* h);
 // Replicates drop out of the lockstep loop as their runs end; afterwards all of them are
 // active again, so that direct hour calls keep working on every world.
 static int run_loop(epi_engine* h) {
+    h->stop_rule = true;
     int rc = run_loop_body(h);
+    h->stop_rule = false;
     int rc2 = set_all_active(h);
     return rc ? rc : rc2;
 }
@@ -566,6 +669,7 @@ static int run_loop_body(epi_engine* h) {
 // ------------------------------------------------------------------ create / destroy
 static void free_device(epi_engine* h) {
     destroy_graphs(h);
+    stream_free(h);
     cudaFree(h->d_params); cudaFree(h->d_chunk_rep); cudaFree(h->d_pos); cudaFree(h->d_home); cudaFree(h->d_work);
     cudaFree(h->d_wsa); cudaFree(h->d_tgt); cudaFree(h->d_lost); cudaFree(h->d_st); cudaFree(h->d_plane); cudaFree(h->d_danger); cudaFree(h->d_claim);
     cudaFree(h->d_counts); cudaFree(h->d_hour_base); cudaFree(h->d_err); cudaFree(h->d_scratch);
@@ -1141,7 +1245,61 @@ int epi_engine_save_state(epi_engine* h) { return h ? save_state(h) : EPI_ERR_AR
 int epi_engine_restore_state(epi_engine* h) { return h ? restore_state(h) : EPI_ERR_ARG; }
 
 int epi_engine_autotune(epi_engine* h, uint32_t hours, epi_launch_shape* chosen) {
-    return h ? autotune(h, hours, chosen) : EPI_ERR_ARG;
+    if (!h) return EPI_ERR_ARG;
+    if (h->stream_file) { h->err = "autotune: close the citizen-state stream first"; return EPI_ERR_ARG; }
+    return autotune(h, hours, chosen);
+}
+
+// Citizen-state stream file: "EPCS", version 1, agents, grid (u32 each); the keyframe (per
+// agent x, y as u16, then every agent's state letter byte); then hour records (stream_write).
+int epi_engine_state_stream_open(epi_engine* h, const char* path) {
+    if (!h || !path) return EPI_ERR_ARG;
+    if (h->R() != 1) { h->err = "the citizen-state stream is for single engines"; return EPI_ERR_ARG; }
+    if (h->stream_file) { h->err = "citizen-state stream already open"; return EPI_ERR_ARG; }
+    const uint32_t n = h->reps[0].n;
+    std::vector<epi_agent_record> recs(n);
+    int rc = snapshot_replica(h, 0, recs.data(), n);
+    if (rc) return rc;
+    FILE* f = std::fopen(path, "wb");
+    if (!f) { h->err = std::string("cannot open ") + path; return EPI_ERR_IO; }
+    const uint32_t head[4] = {0x53435045u /* "EPCS" */, 1u, n, h->reps[0].p.grid_size};
+    std::vector<uint16_t> xy((size_t)n * 2);
+    std::vector<uint8_t> letters(n);
+    for (uint32_t i = 0; i < n; ++i) {
+        xy[2 * i] = (uint16_t)recs[i].x;
+        xy[2 * i + 1] = (uint16_t)recs[i].y;
+        const uint32_t v = recs[i].state;
+        letters[i] = (uint8_t)(v == EPI_S ? 0 : v == EPI_E ? 1 : v == EPI_R ? 3 : v == EPI_D ? 4 : 2);
+    }
+    if (std::fwrite(head, sizeof head, 1, f) != 1 || std::fwrite(xy.data(), sizeof(uint16_t), xy.size(), f) != xy.size() ||
+        std::fwrite(letters.data(), 1, n, f) != n) {
+        std::fclose(f);
+        h->err = "citizen-state stream: write failed";
+        return EPI_ERR_IO;
+    }
+    h->stream_file = f;
+    const size_t cap = (size_t)kStreamChunk * h->slots;
+    CK(cudaMalloc(&h->d_prev, (size_t)h->slots * sizeof(uint32_t)));
+    CK(cudaMalloc(&h->d_codes, cap));
+    CK(cudaMalloc(&h->d_exc, cap * sizeof(uint2)));
+    CK(cudaMalloc(&h->d_exc_n, kStreamChunk * sizeof(uint32_t)));
+    CK(cudaMallocHost(&h->h_codes, cap));
+    CK(cudaMallocHost(&h->h_exc, (size_t)h->slots * sizeof(uint2)));
+    CK(cudaMallocHost(&h->h_exc_n, kStreamChunk * sizeof(uint32_t)));
+    CK(cudaMemcpyAsync(h->d_prev, h->d_pos, (size_t)h->slots * sizeof(uint32_t), cudaMemcpyDeviceToDevice, h->stream));
+    CK(cudaStreamSynchronize(h->stream));
+    destroy_graphs(h);  // hour graphs now carry the encoding kernel
+    return EPI_OK;
+}
+
+int epi_engine_state_stream_close(epi_engine* h) {
+    if (!h) return EPI_ERR_ARG;
+    if (!h->stream_file) return EPI_OK;
+    const int bad = std::fflush(h->stream_file);
+    stream_free(h);
+    destroy_graphs(h);
+    if (bad) { h->err = "citizen-state stream: flush failed"; return EPI_ERR_IO; }
+    return EPI_OK;
 }
 
 int epi_engine_set_launch_shape(epi_engine* h, const epi_launch_shape* shape) {
@@ -1399,14 +1557,14 @@ extern "C" int epi_tick_hour_noalloc(const epi_params* params, uint32_t hour, ui
     const int blocks = (int)std::min<uint64_t>(n_chunks, (uint64_t)d->grid_blocks);
     const uint32_t hod = hour % 24u;
     if (hod >= 1u && hod <= 6u) {
-        k_sleep<<<blocks, kThreads, 0, s>>>(d_params, nullptr, n_chunks, st, counts);
+        k_sleep<<<blocks, kThreads, 0, s>>>(d_params, nullptr, n_chunks, st, counts, nullptr);
     } else {
         NOALLOC_CK(cudaMemsetAsync(d_claim, 0xFF, claim_bytes, s));
         const DecideKernel decide = decide_kernel(hod);
         decide<<<blocks, kThreads, 0, s>>>(d_params, nullptr, n_chunks, pos, st, home, work, work_start_at, plane, nullptr,
-                                           d_claim, d_tgt, nullptr, counts, d_hour, 0u, d_err);
+                                           d_claim, d_tgt, nullptr, counts, d_hour, 0u, d_err, nullptr);
         k_commit<kCommitSlots><<<commit_blocks_for(n), kThreads, 0, s>>>(d_params, nullptr, n, pos, d_tgt, plane, nullptr,
-                                                                         d_claim, nullptr, d_hour, 0u);
+                                                                         d_claim, nullptr, d_hour, 0u, nullptr);
     }
     NOALLOC_CK(cudaGetLastError());
     int err = 0;

@@ -42,6 +42,16 @@ struct BlockRep {
     uint32_t r = 0xFFFFFFFFu;
 };
 
+// The stop rule of run_single_engine (epidemiology_simulation.rs:564-575): a replicate whose
+// last computed counts row (prev, [replicate][8]) has no exposed, infected or hospitalized
+// agent has ended, and the later hours of the segment leave it untouched.  prev is nullptr
+// outside the run loop and for the first hour of a segment.
+__device__ __forceinline__ bool run_ended(const uint32_t* prev, uint32_t r) {
+    if (!prev) return false;
+    const uint32_t* c = prev + (size_t)r * 8u;
+    return (c[1] | c[2] | c[3]) == 0u;
+}
+
 // Switch the block to replicate r: flush the histogram of the previous one into its counts
 // row (counts[r * 8 + bin]), stage r's parameters, clear the histogram.  Block-uniform.
 __device__ __forceinline__ void switch_rep(BlockRep& br, uint32_t r, const DevParams* __restrict__ Pall, DevParams& sP,
@@ -84,14 +94,15 @@ __device__ uint32_t block_first_vacant(const DevParams& P, const PlaneView& pl) 
 
 // Hours 1..6 (SLEEP_START_TIME..=SLEEP_END_TIME, citizen/mod.rs:244-248).
 __global__ void __launch_bounds__(kThreads) k_sleep(const DevParams* __restrict__ Pall, const uint32_t* __restrict__ chunk_rep,
-                                                    uint32_t n_chunks, uint2* __restrict__ st, uint32_t* __restrict__ counts) {
+                                                    uint32_t n_chunks, uint2* __restrict__ st, uint32_t* __restrict__ counts,
+                                                    const uint32_t* __restrict__ prev) {
     __shared__ uint32_t sh[8];
     __shared__ DevParams sP;
     BlockRep br;
     for (uint32_t c = blockIdx.x; c < n_chunks; c += gridDim.x) {
         const uint32_t r = chunk_rep ? chunk_rep[c] : 0u;
         if (r != br.r) switch_rep(br, r, Pall, sP, sh, counts);
-        if (!sP.active) continue;
+        if (!sP.active || run_ended(prev, r)) continue;
         const uint32_t slot = c * kChunk + threadIdx.x;
         const bool valid = slot - sP.agent_off < sP.n;
         uint32_t s = 0;
@@ -117,7 +128,7 @@ __global__ void __launch_bounds__(kThreads) k_decide(const DevParams* __restrict
                                                      uint32_t* __restrict__ claim, uint32_t* __restrict__ tgt,
                                                      uint32_t* __restrict__ lost, uint32_t* __restrict__ counts,
                                                      const uint32_t* __restrict__ hour_base, uint32_t hour_offset,
-                                                     int* err) {
+                                                     int* err, const uint32_t* __restrict__ prev) {
     __shared__ uint32_t sh[8];
     __shared__ DevParams sP;
     const DevParams& P = sP;
@@ -132,7 +143,7 @@ __global__ void __launch_bounds__(kThreads) k_decide(const DevParams* __restrict
             switch_rep(br, r, Pall, sP, sh, counts);
             hosp_known = false;
         }
-        if (!P.active) continue;
+        if (!P.active || run_ended(prev, r)) continue;
         const PlaneView pl{plane + P.plane_off, P.G, P.WP, err, danger ? danger + P.plane_off : nullptr};
         uint32_t* rclaim = claim + P.claim_off;
         const uint32_t slot = c * kChunk + threadIdx.x;
@@ -224,7 +235,8 @@ __global__ void __launch_bounds__(kThreads) k_commit(const DevParams* __restrict
                                                      const uint32_t* __restrict__ tgt, uint8_t* __restrict__ plane,
                                                      uint8_t* __restrict__ danger, const uint32_t* __restrict__ claim,
                                                      const uint32_t* __restrict__ lost,
-                                                     const uint32_t* __restrict__ hour_base, uint32_t hour_offset) {
+                                                     const uint32_t* __restrict__ hour_base, uint32_t hour_offset,
+                                                     const uint32_t* __restrict__ prev) {
     const uint32_t hour = *hour_base + hour_offset;
     const uint32_t base = blockIdx.x * (blockDim.x * S) + threadIdx.x;
     uint32_t t[S], p[S], l[S];
@@ -236,11 +248,12 @@ __global__ void __launch_bounds__(kThreads) k_commit(const DevParams* __restrict
         l[k] = lost && slot < n_slots ? lost[slot] : 0u;
     }
     const DevParams* Pr[S];
-    uint32_t won[S];
+    uint32_t won[S], rr[S];
 #pragma unroll
     for (int k = 0; k < S; ++k) {
         const uint32_t slot = base + k * blockDim.x;
-        Pr[k] = Pall + (chunk_rep && t[k] != kNoAction ? chunk_rep[slot / kChunk] : 0u);
+        rr[k] = chunk_rep && t[k] != kNoAction ? chunk_rep[slot / kChunk] : 0u;
+        Pr[k] = Pall + rr[k];
         won[k] = kNoClaim;  // never equal to a key: stays put
         if (t[k] != kNoAction && target_xy(t[k]) != p[k]) {
             const uint32_t xy = target_xy(t[k]);
@@ -252,7 +265,7 @@ __global__ void __launch_bounds__(kThreads) k_commit(const DevParams* __restrict
     for (int k = 0; k < S; ++k) {
         if (t[k] == kNoAction) continue;
         const DevParams& P = *Pr[k];
-        if (!P.active) continue;
+        if (!P.active || run_ended(prev, rr[k])) continue;
         const uint32_t slot = base + k * blockDim.x;
         const uint32_t i = slot - P.agent_off;
         const uint32_t WP = (uint32_t)P.WP;
@@ -328,6 +341,51 @@ __global__ void k_check_agents(const DevParams* __restrict__ Pall, const uint32_
         const int32_t x = unpack_x(p), y = unpack_y(p);
         if (x > P.G || y > P.G || plane[P.plane_off + (size_t)(y + 1) * P.WP + (x + 1)] != cell_class(P, st[slot].x))
             atomicAdd(bad, 1ull);
+    }
+}
+
+// Citizen-state stream: one byte per agent for the hour -- bits 0-3 the step taken since the
+// previous hour (0 none, 1 + k for the k-th Moore neighbour in NeighborIterator order, 15 a
+// jump recorded as an exception {agent, x | y << 16}), bits 4-6 the state letter
+// (CitizenState::state_str, models/events/citizen_state.rs:33-44: s e i r d = 0..4).
+// prev holds each agent's cell at the previous record.  Single world (slot = agent).
+__device__ __forceinline__ uint32_t state_letter(uint32_t s) {
+    const uint32_t v = s & kStateMask;
+    return v == EPI_S ? 0u : v == EPI_E ? 1u : v == EPI_R ? 3u : v == EPI_D ? 4u : 2u;
+}
+
+__global__ void k_state_delta(uint32_t n, const uint32_t* __restrict__ pos, const uint2* __restrict__ st,
+                              uint32_t* __restrict__ prev, uint8_t* __restrict__ codes, uint2* __restrict__ exc,
+                              uint32_t* __restrict__ exc_count) {
+    const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+    const bool valid = i < n;
+    uint32_t code = 0u, p = 0u;
+    bool jump = false;
+    if (valid) {
+        p = pos[i];
+        const uint32_t q = prev[i];
+        const int32_t dx = unpack_x(p) - unpack_x(q), dy = unpack_y(p) - unpack_y(q);
+        uint32_t step = 0u;
+        if (dx != 0 || dy != 0) {
+            if (dx >= -1 && dx <= 1 && dy >= -1 && dy <= 1) {
+                const int k9 = (dy + 1) * 3 + (dx + 1);     // row-major 3x3 index, centre 4
+                step = 1u + (uint32_t)(k9 < 4 ? k9 : k9 - 1);  // NeighborIterator order
+            } else {
+                step = 15u;
+                jump = true;
+            }
+            prev[i] = p;
+        }
+        code = step | (state_letter(st[i].x) << 4);
+        codes[i] = (uint8_t)code;
+    }
+    // exceptions: one atomic per warp, lanes in order
+    const uint32_t lane = threadIdx.x & 31u, m = __ballot_sync(0xFFFFFFFFu, jump);
+    if (m) {
+        uint32_t base = 0;
+        if (lane == 0) base = atomicAdd(exc_count, (uint32_t)__popc(m));
+        base = __shfl_sync(0xFFFFFFFFu, base, 0);
+        if (jump) exc[base + (uint32_t)__popc(m & ((1u << lane) - 1u))] = make_uint2(i, p);
     }
 }
 

@@ -12,6 +12,7 @@ Every call goes through the C ABI of include/epi_engine.h into the CUDA engine.
 from __future__ import annotations
 
 import ctypes as C
+import os
 import json
 from dataclasses import dataclass
 
@@ -216,6 +217,14 @@ class Epidemiology:
         v = C.c_uint64(0)
         check(lib().epi_engine_kernels_launched(self._h, C.byref(v)), self._h)
         return v.value
+
+    def open_state_stream(self, path: str) -> None:
+        """Record every later hour's citizen states (letter and cell of every agent) to path;
+        epirust_gb300.state_stream.read_state_stream decodes it."""
+        check(lib().epi_engine_state_stream_open(self._h, os.fsencode(path)), self._h)
+
+    def close_state_stream(self) -> None:
+        check(lib().epi_engine_state_stream_close(self._h), self._h)
 
     def autotune(self, hours: int = 24) -> dict:
         """Pick the fastest launch shape over hours 1..hours (state restored afterwards)."""

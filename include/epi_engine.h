@@ -258,6 +258,17 @@ typedef struct {
     double hour_us;          /* autotune: mean wall time of a simulated hour with this shape */
 } epi_launch_shape;
 
+/* Citizen-state stream: the reference's CitizenStatesAtHr messages (every agent's state
+ * letter s/e/i/r/d and cell, every hour; models/events/citizen_state.rs:27-70, published from
+ * allocation_map.rs:122-124 when enable_citizen_state_messages is set) written to a file.
+ * After a keyframe (every agent's cell and letter), each simulated hour is encoded on the
+ * device as one byte per agent -- the Moore step taken (0 none, 1..8 in NeighborIterator
+ * order, 15 a jump listed separately with its cell) and the state letter -- and appended as
+ * {hour, agents, jumps} (u32), the bytes, then the jumps {agent, x | y << 16} in agent order.
+ * epirust_gb300/state_stream.py reads the file back.  Single engines only. */
+int epi_engine_state_stream_open(epi_engine* h, const char* path);
+int epi_engine_state_stream_close(epi_engine* h);
+
 /* Autotuner (no reference counterpart): time hours 1..hours (<= 168) of the current world
  * under each candidate shape -- k_decide grid = resident blocks, twice that, or one chunk per
  * block; 1, 2 or 4 agents per k_commit thread -- from the same starting state, keep the

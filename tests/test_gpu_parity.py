@@ -154,8 +154,8 @@ def test_run_loop_parity(gpu, oracle_mod, name):
     want = rows_to_array(sim.run(1, cfg["hours"], interventions=True, stop=True))
     assert got.shape == want.shape, (got.shape, want.shape)
     assert (got == want).all(), np.nonzero((got != want).any(axis=1))[0][:3]
-    if len(want) == cfg["hours"] - 1:  # no early stop: the final state must match too
-        _assert_same_agents(eng, sim, "end of run")
+    # the final state matches too, also after an early stop (hours after it change nothing)
+    _assert_same_agents(eng, sim, "end of run")
     eng.check_invariants()
 
 
