@@ -24,6 +24,7 @@
 #include "../../include/epi_surrogate.h"
 #include "host.hpp"
 #include "kernels.cuh"
+#include "world.cuh"
 
 using namespace epi;
 using namespace epi::kern;
@@ -729,7 +730,78 @@ static int pack_replica(const epi_engine* h, uint32_t r, const epi_agent_record*
     return EPI_OK;
 }
 
-// Lay out and upload R worlds given as per-replicate record arrays.
+static int finish_upload(epi_engine* h);
+
+// World build on the device (world.cuh) for every replicate, from the host plan.
+static int build_on_device(epi_engine* h) {
+    const uint32_t R = h->R(), n_chunks = h->slots / kChunk;
+    std::vector<WorldDev> W(R);
+    std::vector<uint4> infections;
+    std::vector<WorldPlan> plans(R);
+    std::vector<int> status(R, EPI_OK);
+    std::vector<std::string> errs(R);
+    const unsigned workers = std::max(1u, std::min<unsigned>(R, std::thread::hardware_concurrency()));
+    std::vector<std::thread> pool;
+    for (unsigned w = 0; w < workers; ++w)
+        pool.emplace_back([&, w] {
+            for (uint32_t r = w; r < R; r += workers) status[r] = world_plan(h->reps[r].p, plans[r], errs[r]);
+        });
+    for (auto& t : pool) t.join();
+    for (uint32_t r = 0; r < R; ++r) {
+        if (status[r]) {
+            h->err = (R > 1 ? "replicate " + std::to_string(r) + ": " : std::string()) + errs[r];
+            return status[r];
+        }
+        const WorldPlan& pl = plans[r];
+        const Replica& rep = h->reps[r];
+        WorldDev& d = W[r];
+        d.n = pl.n;
+        d.agent_off = rep.hp.agent_off;
+        d.first_chunk = rep.hp.agent_off / kChunk;
+        d.houses = pl.houses;
+        d.houses_x = pl.geo.houses_x;
+        d.offices = pl.offices;
+        d.offices_x = pl.geo.offices_x;
+        d.hx0 = pl.geo.housing.x0; d.hy0 = pl.geo.housing.y0;
+        d.ox0 = pl.geo.work.x0; d.oy0 = pl.geo.work.y0;
+        d.key0 = pl.key0; d.key1 = pl.key1;
+        d.transport_points = (uint32_t)std::min<uint64_t>(pl.transport_points, 0xFFFFFFFFull);
+        d.thr_work = pl.thr_work; d.thr_pt = pl.thr_pt; d.thr_staff = pl.thr_staff; d.thr_ess = pl.thr_ess;
+        for (const auto& f : pl.infections) infections.push_back(make_uint4(rep.hp.agent_off + f.agent, f.state, f.day, 0u));
+    }
+    WorldDev* d_w = nullptr;
+    uint4* d_inf = nullptr;
+    CK(cudaMalloc(&d_w, R * sizeof(WorldDev)));
+    if (!infections.empty()) CK(cudaMalloc(&d_inf, infections.size() * sizeof(uint4)));
+    int rc = EPI_OK;
+    cudaError_t e = cudaMemcpyAsync(d_w, W.data(), R * sizeof(WorldDev), cudaMemcpyHostToDevice, h->stream);
+    if (e == cudaSuccess && d_inf)
+        e = cudaMemcpyAsync(d_inf, infections.data(), infections.size() * sizeof(uint4), cudaMemcpyHostToDevice, h->stream);
+    if (e == cudaSuccess) {
+        // scratch: d_lost holds the eligibility flags, d_tgt the per-chunk counts (both reset after)
+        const int blocks = (int)std::min<uint64_t>(n_chunks, (uint64_t)h->resident_blocks * 2);
+        k_world_citizens<<<blocks, kThreads, 0, h->stream>>>(d_w, h->d_chunk_rep, n_chunks, h->d_pos, h->d_st, h->d_home,
+                                                             h->d_work, h->d_wsa, h->d_lost, h->d_tgt);
+        k_world_scan<<<1, 1024, 0, h->stream>>>(h->d_tgt, n_chunks);
+        k_world_pt<<<blocks, kThreads, 0, h->stream>>>(d_w, h->d_chunk_rep, n_chunks, h->d_lost, h->d_tgt, h->d_st);
+        if (d_inf)
+            k_world_infect<<<(int)std::min<size_t>((infections.size() + kThreads - 1) / kThreads, 1024), kThreads, 0,
+                             h->stream>>>(d_inf, (uint32_t)infections.size(), h->d_st);
+        e = cudaGetLastError();
+        if (e == cudaSuccess) e = cudaStreamSynchronize(h->stream);
+        h->kernels_launched += d_inf ? 4 : 3;
+    }
+    if (e != cudaSuccess) {
+        h->err = std::string("device world build: ") + cudaGetErrorString(e);
+        rc = EPI_ERR_CUDA;
+    }
+    cudaFree(d_w);
+    cudaFree(d_inf);
+    return rc;
+}
+
+// Lay out and upload R worlds given as per-replicate record arrays (nullptr: build them on
+// the device).
 static int engine_init(epi_engine* h, const epi_params* params, const epi_agent_record* const* recs, uint32_t R) {
     if (R == 0) { h->err = "no replicates"; return EPI_ERR_ARG; }
     h->reps.resize(R);
@@ -794,6 +866,11 @@ static int engine_init(epi_engine* h, const epi_params* params, const epi_agent_
     CK(cudaMallocHost(&h->h_hour_base, sizeof(uint32_t)));
     int rc = ensure_counts(h, 48);
     if (rc) return rc;
+    if (!recs) {
+        rc = build_on_device(h);
+        if (rc) return rc;
+        return finish_upload(h);
+    }
     // host mirrors, filled per replicate (in parallel for large ensembles)
     std::vector<uint32_t> pos(slots, 0), home(slots, 0), work(slots, 0), wsa(slots, 0);
     std::vector<uint2> st(slots, make_uint2(0, 0));
@@ -814,45 +891,28 @@ static int engine_init(epi_engine* h, const epi_params* params, const epi_agent_
     CK(cudaMemcpyAsync(h->d_work, work.data(), slots * sizeof(uint32_t), cudaMemcpyHostToDevice, h->stream));
     CK(cudaMemcpyAsync(h->d_wsa, wsa.data(), slots * sizeof(uint32_t), cudaMemcpyHostToDevice, h->stream));
     CK(cudaMemcpyAsync(h->d_st, st.data(), slots * sizeof(uint2), cudaMemcpyHostToDevice, h->stream));
+    CK(cudaStreamSynchronize(h->stream));  // the host mirrors go out of scope
+    return finish_upload(h);
+}
+
+// Everything after the agent arrays are on the device: scratch words, planes, parameters.
+static int finish_upload(epi_engine* h) {
+    const size_t slots = h->slots;
     CK(cudaMemsetAsync(h->d_tgt, 0xFF, slots * sizeof(uint32_t), h->stream));
     CK(cudaMemsetAsync(h->d_lost, 0xFF, slots * sizeof(uint32_t), h->stream));
     CK(cudaMemsetAsync(h->d_plane, 0, h->plane_bytes, h->stream));
     CK(cudaMemsetAsync(h->d_danger, 0, h->plane_bytes, h->stream));
     CK(cudaMemsetAsync(h->d_claim, 0xFF, h->claim_cells * sizeof(uint32_t), h->stream));
     CK(cudaMemsetAsync(h->d_err, 0, sizeof(int), h->stream));
-    rc = push_params(h);
+    int rc = push_params(h);
     if (rc) return rc;
     LAUNCH(kKBuildPlane, (k_build_plane<<<blocks_for(h->slots), kThreads, 0, h->stream>>>(
                               h->d_params, h->d_chunk_rep, h->slots, h->d_pos, h->d_st, h->d_plane, h->d_danger,
                               h->d_err)));
-    CK(cudaStreamSynchronize(h->stream));  // the host mirrors go out of scope
+    CK(cudaStreamSynchronize(h->stream));
     rc = harvest_events(h);
     if (rc) return rc;
     return check_error_flag(h);
-}
-
-// World builds of R configurations on the host, in parallel.
-static int build_worlds(const epi_params* params, uint32_t R, std::vector<std::vector<epi_agent_record>>& worlds,
-                        std::string& err) {
-    worlds.assign(R, {});
-    std::vector<int> status(R, EPI_OK);
-    std::vector<std::string> errs(R);
-    const unsigned workers = std::max(1u, std::min<unsigned>(R, std::thread::hardware_concurrency()));
-    std::vector<std::thread> pool;
-    for (unsigned w = 0; w < workers; ++w)
-        pool.emplace_back([&, w] {
-            for (uint32_t r = w; r < R; r += workers) {
-                epi_geography g;
-                status[r] = build_world(params[r], worlds[r], g, errs[r]);
-            }
-        });
-    for (auto& t : pool) t.join();
-    for (uint32_t r = 0; r < R; ++r)
-        if (status[r]) {
-            err = (R > 1 ? "replicate " + std::to_string(r) + ": " : std::string()) + errs[r];
-            return status[r];
-        }
-    return EPI_OK;
 }
 
 static int snapshot_replica(epi_engine* h, uint32_t r, epi_agent_record* out, size_t n) {
@@ -1128,11 +1188,7 @@ int epi_engine_create_from_records(const epi_params* params, const epi_agent_rec
 int epi_engine_create(const epi_params* params, epi_engine** out) {
     if (!params || !out) return EPI_ERR_ARG;
     *out = nullptr;
-    std::vector<std::vector<epi_agent_record>> worlds;
-    std::string err;
-    int rc = build_worlds(params, 1, worlds, err);
-    if (rc) { g_create_error = err; return rc; }
-    return epi_engine_create_from_records(params, worlds[0].data(), worlds[0].size(), out);
+    return create_engine(params, nullptr, 1, out);
 }
 
 int epi_engine_create_json(const char* config_json, uint64_t seed, epi_engine** out) {
@@ -1369,14 +1425,8 @@ int epi_engine_hour_bytes(const epi_engine* h, uint32_t hour, double* bytes) {
 int epi_ensemble_create(const epi_params* params, uint32_t replicates, epi_ensemble** out) {
     if (!params || !out || replicates == 0) return EPI_ERR_ARG;
     *out = nullptr;
-    std::vector<std::vector<epi_agent_record>> worlds;
-    std::string err;
-    int rc = build_worlds(params, replicates, worlds, err);
-    if (rc) { g_create_error = err; return rc; }
-    std::vector<const epi_agent_record*> recs(replicates);
-    for (uint32_t r = 0; r < replicates; ++r) recs[r] = worlds[r].data();
     epi_ensemble* e = new epi_ensemble();
-    rc = engine_init(&e->core, params, recs.data(), replicates);
+    int rc = engine_init(&e->core, params, nullptr, replicates);
     if (rc) {
         g_create_error = e->core.err;
         free_device(&e->core);

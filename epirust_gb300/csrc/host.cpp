@@ -9,6 +9,7 @@
 #include <cstring>
 #include <ctime>
 #include <stdexcept>
+#include <unordered_map>
 
 #include "json.hpp"
 
@@ -211,15 +212,17 @@ inline bool bern(uint32_t u, uint64_t thr) { return (uint64_t)u < thr; }
 //     the k-th (by index) takes the k-th cell of the x-major product of the house's two
 //     columns and two rows (Area::random_points over a 2x2 house);
 //   - resize_hospital(N, 0.002, beds), then Normal workers become Essential ~ B(ess).
-int build_world(const epi_params& p, std::vector<epi_agent_record>& out, epi_geography& geo, std::string& err) {
+int world_plan(const epi_params& p, WorldPlan& plan, std::string& err) {
     std::string bad = validate_params(p);
     if (!bad.empty()) { err = bad; return EPI_ERR_CONFIG; }
-    geo = define_geography(p.grid_size);
+    plan.geo = define_geography(p.grid_size);
+    const epi_geography& geo = plan.geo;
     const uint32_t n = p.number_of_agents;
-    const uint32_t houses = geo.houses_x * geo.houses_y;
-    const uint32_t offices = geo.offices_x * geo.offices_y;
-    if (houses == 0 || offices == 0) { err = "grid too small: no houses or no offices"; return EPI_ERR_CONFIG; }
-    const uint64_t per_house = ((uint64_t)n + houses - 1) / houses;
+    plan.n = n;
+    plan.houses = geo.houses_x * geo.houses_y;
+    plan.offices = geo.offices_x * geo.offices_y;
+    if (plan.houses == 0 || plan.offices == 0) { err = "grid too small: no houses or no offices"; return EPI_ERR_CONFIG; }
+    const uint64_t per_house = ((uint64_t)n + plan.houses - 1) / plan.houses;
     if (per_house > 4) {
         err = "There are " + std::to_string(per_house) + " agents assigned to a house, but house capacity is 4";
         return EPI_ERR_CAPACITY;
@@ -229,7 +232,9 @@ int build_world(const epi_params& p, std::vector<epi_agent_record>& out, epi_geo
         err = "There are " + std::to_string(infections) + " people set to infect, but only " + std::to_string(n) + " agents available";
         return EPI_ERR_CAPACITY;
     }
-    WorldDraws wd{(uint32_t)p.seed, (uint32_t)(p.seed >> 32)};
+    plan.key0 = (uint32_t)p.seed;
+    plan.key1 = (uint32_t)(p.seed >> 32);
+    WorldDraws wd{plan.key0, plan.key1};
 
     // Number of transport points: min(n_pt, |xs| * |ys|) of Area::random_points.
     const double wanted = (double)n * (p.public_transport_percentage + 0.1) * (p.working_percentage + 0.1);
@@ -239,11 +244,49 @@ int build_world(const epi_params& p, std::vector<epi_agent_record>& out, epi_geo
     uint64_t rows = (uint64_t)(geo.transport.y1 - geo.transport.y0 + 1);
     cols = cols < side ? cols : side;
     rows = rows < side ? rows : side;
-    const uint64_t transport_points = cols * rows < n_points ? cols * rows : n_points;
+    plan.transport_points = cols * rows < n_points ? cols * rows : n_points;
 
-    const uint64_t thr_work = bernoulli_threshold(p.working_percentage);
-    const uint64_t thr_pt = bernoulli_threshold(p.public_transport_percentage);
-    const uint64_t thr_staff = bernoulli_threshold(0.002);
+    plan.thr_work = bernoulli_threshold(p.working_percentage);
+    plan.thr_pt = bernoulli_threshold(p.public_transport_percentage);
+    plan.thr_staff = bernoulli_threshold(0.002);
+    plan.thr_ess = bernoulli_threshold(p.has_lockdown ? p.essential_workers_population : 0.0);
+
+    // set_starting_infections: choose_multiple as a partial Fisher-Yates shuffle of the agent
+    // indices (only the touched positions are stored), then the exposed, asymptomatic, mild
+    // and severe agents in that order
+    plan.infections.clear();
+    if (infections) {
+        std::unordered_map<uint32_t, uint32_t> moved;  // position -> agent, where not the identity
+        auto at = [&](uint32_t k) { auto it = moved.find(k); return it == moved.end() ? k : it->second; };
+        std::vector<uint32_t> picked((size_t)infections);
+        for (uint32_t j = 0; j < (uint32_t)infections; ++j) {
+            uint32_t u[4];
+            wd.at(j, kBlkInfectPick, u);
+            const uint32_t r = j + uniform_index(u[0], n - j);
+            const uint32_t aj = at(j), ar = at(r);
+            moved[j] = ar;
+            moved[r] = aj;
+            picked[j] = ar;
+        }
+        uint32_t j = 0;
+        auto set = [&](uint32_t count, uint8_t state, uint32_t day) {
+            for (uint32_t k = 0; k < count; ++k, ++j) plan.infections.push_back({picked[j], state, day});
+        };
+        set(p.exposed, EPI_E, 0);
+        set(p.infected_mild_asymptomatic, EPI_I_ASYM, 1);
+        set(p.infected_mild_symptomatic, EPI_I_MILD, 1);
+        set(p.infected_severe, EPI_I_SEVERE, 1);
+    }
+    return EPI_OK;
+}
+
+int build_world(const epi_params& p, std::vector<epi_agent_record>& out, epi_geography& geo, std::string& err) {
+    WorldPlan plan;
+    int rc = world_plan(p, plan, err);
+    if (rc) return rc;
+    geo = plan.geo;
+    const uint32_t n = plan.n, houses = plan.houses, offices = plan.offices;
+    WorldDraws wd{plan.key0, plan.key1};
     out.assign(n, epi_agent_record());
     uint64_t pt_users = 0;
     for (uint32_t i = 0; i < n; ++i) {
@@ -251,16 +294,16 @@ int build_world(const epi_params& p, std::vector<epi_agent_record>& out, epi_geo
         wd.at(i, kBlkCitizen, u);
         epi_agent_record& r = out[i];
         std::memset(&r, 0, sizeof r);
-        const bool working = bern(u[0], thr_work);
+        const bool working = bern(u[0], plan.thr_work);
         const epi_area h = house_area(geo, i % houses);
         const epi_area o = office_area(geo, i % offices);
-        const bool pt = bern(u[1], thr_pt) && working && pt_users < transport_points;
+        const bool pt = bern(u[1], plan.thr_pt) && working && pt_users < plan.transport_points;
         if (pt) ++pt_users;
         r.flags = pt ? EPI_F_PUBLIC_TRANSPORT : 0;
         r.home_x = h.x0; r.home_y = h.y0;
         if (working) {
             r.work_x = o.x0; r.work_y = o.y0;
-            if (bern(u[2], thr_staff)) { r.work_status = EPI_WS_HOSPITAL_STAFF; r.work_start_at = 8; }
+            if (bern(u[2], plan.thr_staff)) { r.work_status = EPI_WS_HOSPITAL_STAFF; r.work_start_at = 8; }
             else r.work_status = EPI_WS_NORMAL;
         } else {
             r.work_x = h.x0; r.work_y = h.y0;
@@ -270,30 +313,11 @@ int build_world(const epi_params& p, std::vector<epi_agent_record>& out, epi_geo
         r.state = EPI_S;
         r.area_x0 = h.x0; r.area_y0 = h.y0; r.area_x1 = h.x1; r.area_y1 = h.y1;
     }
-
-    if (infections) {
-        std::vector<uint32_t> order(n);
-        for (uint32_t i = 0; i < n; ++i) order[i] = i;
-        for (uint32_t j = 0; j < (uint32_t)infections; ++j) {
-            uint32_t u[4];
-            wd.at(j, kBlkInfectPick, u);
-            uint32_t r = j + uniform_index(u[0], n - j);
-            std::swap(order[j], order[r]);
-        }
-        uint32_t j = 0;
-        auto set = [&](uint32_t count, uint8_t state, uint32_t day) {
-            for (uint32_t k = 0; k < count; ++k, ++j) {
-                out[order[j]].state = state;
-                out[order[j]].infection_day = day;
-                out[order[j]].at_hour = 0;
-            }
-        };
-        set(p.exposed, EPI_E, 0);
-        set(p.infected_mild_asymptomatic, EPI_I_ASYM, 1);
-        set(p.infected_mild_symptomatic, EPI_I_MILD, 1);
-        set(p.infected_severe, EPI_I_SEVERE, 1);
+    for (const auto& inf : plan.infections) {
+        out[inf.agent].state = inf.state;
+        out[inf.agent].infection_day = inf.day;
+        out[inf.agent].at_hour = 0;
     }
-
     for (uint32_t i = 0; i < n; ++i) {
         const uint32_t house = i % houses, rank = i / houses;
         const uint32_t in_house = (n - 1 - house) / houses + 1;
@@ -308,15 +332,12 @@ int build_world(const epi_params& p, std::vector<epi_agent_record>& out, epi_geo
             r.y = r.home_y + (int32_t)(rank & 1u);
         }
     }
-
     resize_hospital(geo, (int32_t)n, 0.002, p.hospital_beds_percentage);
-
-    const uint64_t thr_ess = bernoulli_threshold(p.has_lockdown ? p.essential_workers_population : 0.0);
     for (uint32_t i = 0; i < n; ++i) {
         if (out[i].work_status != EPI_WS_NORMAL) continue;
         uint32_t u[4];
         wd.at(i, kBlkEssential, u);
-        if (bern(u[0], thr_ess)) out[i].work_status = EPI_WS_ESSENTIAL;
+        if (bern(u[0], plan.thr_ess)) out[i].work_status = EPI_WS_ESSENTIAL;
     }
     return EPI_OK;
 }

@@ -25,6 +25,21 @@ epi_area office_area(const epi_geography& g, uint32_t k);
 // start points, hospital resize, essential workers).  Returns EPI_OK or an error code.
 int build_world(const epi_params& p, std::vector<epi_agent_record>& out, epi_geography& geo, std::string& err);
 
+// Everything about a world build that is not per agent: the checks of generate_population
+// and set_starting_infections, the Bernoulli thresholds, the public-transport budget of
+// Area::random_points and the starting infections (agent index, state, infection day) in
+// the order set_starting_infections assigns them.  build_world and the device build share it.
+struct WorldPlan {
+    epi_geography geo{};  // before resize_hospital
+    uint32_t n = 0, houses = 0, offices = 0;
+    uint64_t transport_points = 0;
+    uint64_t thr_work = 0, thr_pt = 0, thr_staff = 0, thr_ess = 0;
+    uint32_t key0 = 0, key1 = 0;
+    struct Infection { uint32_t agent; uint8_t state; uint32_t day; };
+    std::vector<Infection> infections;
+};
+int world_plan(const epi_params& p, WorldPlan& plan, std::string& err);
+
 struct Report {
     uint32_t hour;
     std::string name, data;
