@@ -59,6 +59,8 @@ class EpiParams(C.Structure):
         ("vaccination_percent", C.c_double * MAX_VACCINATIONS),
         ("hospital_occupancy_trigger", C.c_double),
         ("seed", C.c_uint64),
+        ("population_source", C.c_uint32),
+        ("population_file", C.c_char * 256),
     ]
 
 
@@ -106,6 +108,7 @@ EXPORTS = [
     "epi_ensemble_save_state", "epi_ensemble_restore_state", "epi_ensemble_set_profiling", "epi_ensemble_kernel_stats",
     "epi_ensemble_kernels_launched", "epi_ensemble_hour_bytes", "epi_engine_autotune", "epi_engine_set_launch_shape",
     "epi_engine_launch_shape", "epi_ensemble_autotune", "epi_engine_state_stream_open", "epi_engine_state_stream_close",
+    "epi_population_read_csv", "epi_world_build_population", "epi_engine_create_population",
 ]
 
 
@@ -207,6 +210,9 @@ def lib():
     _sig(L, "epi_ensemble_autotune", C.c_int, [V, C.c_uint32, P(LaunchShape)])
     _sig(L, "epi_engine_state_stream_open", C.c_int, [V, C.c_char_p])
     _sig(L, "epi_engine_state_stream_close", C.c_int, [V])
+    _sig(L, "epi_population_read_csv", C.c_int, [C.c_char_p, V, C.c_uint32, P(C.c_uint32)])
+    _sig(L, "epi_world_build_population", C.c_int, [P(EpiParams), V, C.c_uint32, V, P(EpiGeography)])
+    _sig(L, "epi_engine_create_population", C.c_int, [P(EpiParams), V, C.c_uint32, P(V)])
     F = P(C.c_float)
     _sig(L, "epi_mlp_create", C.c_int, [P(MlpConfig), P(V)])
     _sig(L, "epi_mlp_destroy", C.c_int, [V])

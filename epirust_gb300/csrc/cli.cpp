@@ -66,7 +66,16 @@ int main(int argc, char** argv) {
     }
     auto t0 = std::chrono::steady_clock::now();
     epi_engine* h = nullptr;
-    int rc = epi_engine_create(&p, &h);
+    int rc;
+    if (p.population_source == 1) {  // Population::Csv: the rows of its file
+        uint32_t n = 0;
+        rc = epi_population_read_csv(p.population_file, nullptr, 0, &n);
+        std::vector<uint8_t> flags(n);
+        if (rc == EPI_OK) rc = epi_population_read_csv(p.population_file, flags.data(), n, &n);
+        if (rc == EPI_OK) rc = epi_engine_create_population(&p, flags.data(), n, &h);
+    } else {
+        rc = epi_engine_create(&p, &h);
+    }
     if (rc != EPI_OK) { std::fprintf(stderr, "engine create failed (%d): %s\n", rc, epi_engine_last_error(nullptr)); return 1; }
     if (citizen_states) {
         const std::string dir = out_dir + "/output";

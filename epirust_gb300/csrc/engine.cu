@@ -100,6 +100,7 @@ struct epi_engine {
     uint64_t kernels_launched = 0;
     int64_t last_claim_hour = -1;  // latest hour whose claims may sit in the claim plane (-1: clean)
     bool stop_rule = false;        // inside the run loop: hours after a replicate's stop do nothing
+    const uint8_t* init_flags = nullptr;  // during creation: Csv population flags of replicate 0
     // citizen-state stream (single world): per-hour codes written by k_state_delta
     FILE* stream_file = nullptr;
     uint32_t* d_prev = nullptr;     // cell of every agent at the previous record
@@ -744,7 +745,15 @@ static int build_on_device(epi_engine* h) {
     std::vector<std::thread> pool;
     for (unsigned w = 0; w < workers; ++w)
         pool.emplace_back([&, w] {
-            for (uint32_t r = w; r < R; r += workers) status[r] = world_plan(h->reps[r].p, plans[r], errs[r]);
+            for (uint32_t r = w; r < R; r += workers) {
+                const bool csv = h->reps[r].p.population_source == 1;
+                if (csv && (R != 1 || !h->init_flags)) {
+                    status[r] = EPI_ERR_ARG;
+                    errs[r] = "a Csv population comes with its rows (epi_engine_create_population, single engines)";
+                    continue;
+                }
+                status[r] = world_plan(h->reps[r].p, plans[r], errs[r], csv ? h->init_flags : nullptr);
+            }
         });
     for (auto& t : pool) t.join();
     for (uint32_t r = 0; r < R; ++r) {
@@ -766,12 +775,19 @@ static int build_on_device(epi_engine* h) {
         d.ox0 = pl.geo.work.x0; d.oy0 = pl.geo.work.y0;
         d.key0 = pl.key0; d.key1 = pl.key1;
         d.transport_points = (uint32_t)std::min<uint64_t>(pl.transport_points, 0xFFFFFFFFull);
+        d.csv = pl.flags ? 1u : 0u;
         d.thr_work = pl.thr_work; d.thr_pt = pl.thr_pt; d.thr_staff = pl.thr_staff; d.thr_ess = pl.thr_ess;
         for (const auto& f : pl.infections) infections.push_back(make_uint4(rep.hp.agent_off + f.agent, f.state, f.day, 0u));
     }
     WorldDev* d_w = nullptr;
     uint4* d_inf = nullptr;
+    uint8_t* d_flags = nullptr;
     CK(cudaMalloc(&d_w, R * sizeof(WorldDev)));
+    if (h->init_flags) {  // single Csv world: slot = agent
+        CK(cudaMalloc(&d_flags, h->slots));
+        CK(cudaMemsetAsync(d_flags, 0, h->slots, h->stream));
+        CK(cudaMemcpyAsync(d_flags, h->init_flags, h->reps[0].n, cudaMemcpyHostToDevice, h->stream));
+    }
     if (!infections.empty()) CK(cudaMalloc(&d_inf, infections.size() * sizeof(uint4)));
     int rc = EPI_OK;
     cudaError_t e = cudaMemcpyAsync(d_w, W.data(), R * sizeof(WorldDev), cudaMemcpyHostToDevice, h->stream);
@@ -781,7 +797,7 @@ static int build_on_device(epi_engine* h) {
         // scratch: d_lost holds the eligibility flags, d_tgt the per-chunk counts (both reset after)
         const int blocks = (int)std::min<uint64_t>(n_chunks, (uint64_t)h->resident_blocks * 2);
         k_world_citizens<<<blocks, kThreads, 0, h->stream>>>(d_w, h->d_chunk_rep, n_chunks, h->d_pos, h->d_st, h->d_home,
-                                                             h->d_work, h->d_wsa, h->d_lost, h->d_tgt);
+                                                             h->d_work, h->d_wsa, h->d_lost, h->d_tgt, d_flags);
         k_world_scan<<<1, 1024, 0, h->stream>>>(h->d_tgt, n_chunks);
         k_world_pt<<<blocks, kThreads, 0, h->stream>>>(d_w, h->d_chunk_rep, n_chunks, h->d_lost, h->d_tgt, h->d_st);
         if (d_inf)
@@ -797,6 +813,7 @@ static int build_on_device(epi_engine* h) {
     }
     cudaFree(d_w);
     cudaFree(d_inf);
+    cudaFree(d_flags);
     return rc;
 }
 
@@ -1161,8 +1178,52 @@ int epi_disease_is_to_be_hospitalized(const epi_params* p, uint32_t day) {
     return epi_disease_transmission_rate(p, day) >= p->high_transmission_rate;
 }
 
+int epi_population_read_csv(const char* path, uint8_t* flags, uint32_t cap, uint32_t* n) {
+    if (!path || !n) return EPI_ERR_ARG;
+    std::vector<uint8_t> f;
+    std::string err;
+    int rc = read_population_csv(path, f, err);
+    if (rc) { g_create_error = err; return rc; }
+    *n = (uint32_t)f.size();
+    if (flags) std::memcpy(flags, f.data(), std::min<size_t>(f.size(), cap));
+    return EPI_OK;
+}
+
+int epi_world_build_population(const epi_params* p, const uint8_t* flags, uint32_t n, epi_agent_record* out,
+                               epi_geography* geo) {
+    if (!p || !flags || !out || n != p->number_of_agents) return EPI_ERR_ARG;
+    std::vector<epi_agent_record> recs;
+    epi_geography g;
+    std::string err;
+    int rc = build_world(*p, recs, g, err, flags);
+    if (rc) { g_create_error = err; return rc; }
+    std::memcpy(out, recs.data(), (size_t)n * sizeof(epi_agent_record));
+    if (geo) *geo = g;
+    return EPI_OK;
+}
+
+int epi_engine_create_population(const epi_params* params, const uint8_t* flags, uint32_t n, epi_engine** out) {
+    if (!params || !flags || !out || n != params->number_of_agents) return EPI_ERR_ARG;
+    *out = nullptr;
+    epi_params p = *params;
+    p.population_source = 1;
+    epi_engine* h = new epi_engine();
+    h->init_flags = flags;
+    int rc = engine_init(h, &p, nullptr, 1);
+    h->init_flags = nullptr;
+    if (rc) {
+        g_create_error = h->err;
+        free_device(h);
+        delete h;
+        return rc;
+    }
+    *out = h;
+    return EPI_OK;
+}
+
 int epi_world_build(const epi_params* p, epi_agent_record* out, size_t n, epi_geography* geo) {
     if (!p || !out || n != p->number_of_agents) return EPI_ERR_ARG;
+    if (p->population_source == 1) { g_create_error = "Csv population: use epi_world_build_population"; return EPI_ERR_ARG; }
     std::vector<epi_agent_record> recs;
     epi_geography g;
     std::string err;
@@ -1199,6 +1260,13 @@ int epi_engine_create_json(const char* config_json, uint64_t seed, epi_engine** 
     int rc = epi_params_from_json(config_json, &p, msg, sizeof msg);
     if (rc) { g_create_error = msg; return rc; }
     p.seed = seed;
+    if (p.population_source == 1) {  // Population::Csv: read the rows of its file
+        std::vector<uint8_t> flags;
+        std::string err;
+        rc = read_population_csv(p.population_file, flags, err);
+        if (rc) { g_create_error = err; return rc; }
+        return epi_engine_create_population(&p, flags.data(), (uint32_t)flags.size(), out);
+    }
     return epi_engine_create(&p, out);
 }
 

@@ -35,6 +35,65 @@ uint32_t as_u32(const json::Value& v, const char* what) {
 // GeographyParameters, hours, interventions and starting_infections (default: 1 exposed,
 // common/src/config/starting_infections.rs:65-69).  Two optional keys that the reference
 // ignores select the random stream ("seed") and the occupancy-triggered hospital build.
+int read_population_csv(const std::string& path, std::vector<uint8_t>& flags, std::string& err) {
+    FILE* f = std::fopen(path.c_str(), "rb");
+    if (!f) { err = "Could not read population file " + path; return EPI_ERR_IO; }
+    std::string text;
+    char buf[1 << 16];
+    size_t got;
+    while ((got = std::fread(buf, 1, sizeof buf, f)) > 0) text.append(buf, got);
+    std::fclose(f);
+    auto split = [](const std::string& line) {
+        std::vector<std::string> out;
+        size_t a = 0;
+        while (true) {
+            size_t b = line.find(',', a);
+            std::string cell = line.substr(a, b == std::string::npos ? std::string::npos : b - a);
+            while (!cell.empty() && (cell.back() == '\r' || cell.back() == ' ')) cell.pop_back();
+            while (!cell.empty() && cell.front() == ' ') cell.erase(cell.begin());
+            out.push_back(cell);
+            if (b == std::string::npos) break;
+            a = b + 1;
+        }
+        return out;
+    };
+    flags.clear();
+    size_t pos = 0;
+    int col_work = -1, col_pt = -1;
+    size_t line_no = 0;
+    while (pos < text.size()) {
+        size_t end = text.find('\n', pos);
+        if (end == std::string::npos) end = text.size();
+        const std::string line = text.substr(pos, end - pos);
+        pos = end + 1;
+        ++line_no;
+        if (line.find_first_not_of(" \r") == std::string::npos) continue;
+        const std::vector<std::string> cells = split(line);
+        if (col_work < 0) {  // the header row names the PopulationRecord fields
+            for (size_t c = 0; c < cells.size(); ++c) {
+                if (cells[c] == "working") col_work = (int)c;
+                if (cells[c] == "pub_transport") col_pt = (int)c;
+            }
+            if (col_work < 0 || col_pt < 0) { err = path + ": the header needs the columns working and pub_transport"; return EPI_ERR_CONFIG; }
+            continue;
+        }
+        auto boolean = [&](int c, uint8_t bit) -> int {
+            if ((size_t)c >= cells.size()) return -1;
+            if (cells[c] == "True") return bit;
+            if (cells[c] == "False") return 0;
+            return -1;
+        };
+        const int w = boolean(col_work, 1), t = boolean(col_pt, 2);
+        if (w < 0 || t < 0) {
+            err = path + ":" + std::to_string(line_no) + ": working and pub_transport must be True or False";
+            return EPI_ERR_CONFIG;
+        }
+        flags.push_back((uint8_t)(w | t));
+    }
+    if (flags.empty()) { err = path + ": no citizens"; return EPI_ERR_CONFIG; }
+    return EPI_OK;
+}
+
 epi_params params_from_json(const std::string& text) {
     json::Value root = json::parse(text);
     if (root.kind != json::Value::Object) throw std::runtime_error("config must be a JSON object");
@@ -42,11 +101,23 @@ epi_params params_from_json(const std::string& text) {
     std::memset(&p, 0, sizeof p);
 
     const json::Value& pop = need(root, "population", "config");
-    if (pop.get("Csv")) throw std::runtime_error("Csv population is not supported by this engine (use Auto)");
-    const json::Value& autop = need(pop, "Auto", "population");
-    p.number_of_agents = as_u32(need(autop, "number_of_agents", "Auto"), "number_of_agents");
-    p.public_transport_percentage = need(autop, "public_transport_percentage", "Auto").as_double();
-    p.working_percentage = need(autop, "working_percentage", "Auto").as_double();
+    if (const json::Value* csv = pop.get("Csv")) {
+        // Population::Csv{file, cols}: the agent count is the file's row count
+        const json::Value& file = need(*csv, "file", "Csv");
+        if (file.kind != json::Value::String || file.text.empty() || file.text.size() >= sizeof p.population_file)
+            throw std::runtime_error("Csv.file must be a path shorter than 256 bytes");
+        std::memcpy(p.population_file, file.text.c_str(), file.text.size() + 1);
+        p.population_source = 1;
+        std::vector<uint8_t> flags;
+        std::string err;
+        if (read_population_csv(file.text, flags, err)) throw std::runtime_error(err);
+        p.number_of_agents = (uint32_t)flags.size();
+    } else {
+        const json::Value& autop = need(pop, "Auto", "population");
+        p.number_of_agents = as_u32(need(autop, "number_of_agents", "Auto"), "number_of_agents");
+        p.public_transport_percentage = need(autop, "public_transport_percentage", "Auto").as_double();
+        p.working_percentage = need(autop, "working_percentage", "Auto").as_double();
+    }
 
     const json::Value* dis = root.get("disease");
     if (!dis || dis->kind != json::Value::Object)
@@ -114,6 +185,7 @@ epi_params params_from_json(const std::string& text) {
 std::string validate_params(const epi_params& p) {
     auto pct = [](double v) { return v >= 0.0 && v <= 1.0; };  // validate_percentage, custom_types.rs:29-35
     if (p.number_of_agents == 0) return "population is empty (No citizens!)";
+    if (p.population_source > 1) return "population_source must be 0 (Auto) or 1 (Csv)";
     if (p.number_of_agents > kMaxAgentsPerWorld) return "number_of_agents must be <= 33554431 per world";
     if (p.grid_size < 1 || p.grid_size > kMaxGrid) return "grid_size must be in [1, 16382]";
     if (p.hours > kMaxHours) return "hours must be <= 1500000 (16-bit infection day on the device)";
@@ -212,7 +284,7 @@ inline bool bern(uint32_t u, uint64_t thr) { return (uint64_t)u < thr; }
 //     the k-th (by index) takes the k-th cell of the x-major product of the house's two
 //     columns and two rows (Area::random_points over a 2x2 house);
 //   - resize_hospital(N, 0.002, beds), then Normal workers become Essential ~ B(ess).
-int world_plan(const epi_params& p, WorldPlan& plan, std::string& err) {
+int world_plan(const epi_params& p, WorldPlan& plan, std::string& err, const uint8_t* flags) {
     std::string bad = validate_params(p);
     if (!bad.empty()) { err = bad; return EPI_ERR_CONFIG; }
     plan.geo = define_geography(p.grid_size);
@@ -222,6 +294,12 @@ int world_plan(const epi_params& p, WorldPlan& plan, std::string& err) {
     plan.houses = geo.houses_x * geo.houses_y;
     plan.offices = geo.offices_x * geo.offices_y;
     if (plan.houses == 0 || plan.offices == 0) { err = "grid too small: no houses or no offices"; return EPI_ERR_CONFIG; }
+    plan.flags = flags;
+    if (flags && (uint64_t)n > 4ull * plan.houses) {  // read_population, grid.rs:216-223
+        err = "Cannot accommodate citizens into homes! There are " + std::to_string(n) + " citizens, but " +
+              std::to_string(4ull * plan.houses) + " home points";
+        return EPI_ERR_CAPACITY;
+    }
     const uint64_t per_house = ((uint64_t)n + plan.houses - 1) / plan.houses;
     if (per_house > 4) {
         err = "There are " + std::to_string(per_house) + " agents assigned to a house, but house capacity is 4";
@@ -280,9 +358,10 @@ int world_plan(const epi_params& p, WorldPlan& plan, std::string& err) {
     return EPI_OK;
 }
 
-int build_world(const epi_params& p, std::vector<epi_agent_record>& out, epi_geography& geo, std::string& err) {
+int build_world(const epi_params& p, std::vector<epi_agent_record>& out, epi_geography& geo, std::string& err,
+                const uint8_t* flags) {
     WorldPlan plan;
-    int rc = world_plan(p, plan, err);
+    int rc = world_plan(p, plan, err, flags);
     if (rc) return rc;
     geo = plan.geo;
     const uint32_t n = plan.n, houses = plan.houses, offices = plan.offices;
@@ -294,11 +373,16 @@ int build_world(const epi_params& p, std::vector<epi_agent_record>& out, epi_geo
         wd.at(i, kBlkCitizen, u);
         epi_agent_record& r = out[i];
         std::memset(&r, 0, sizeof r);
-        const bool working = bern(u[0], plan.thr_work);
+        const bool working = flags ? (flags[i] & 1u) != 0 : bern(u[0], plan.thr_work);
         const epi_area h = house_area(geo, i % houses);
         const epi_area o = office_area(geo, i % offices);
-        const bool pt = bern(u[1], plan.thr_pt) && working && pt_users < plan.transport_points;
-        if (pt) ++pt_users;
+        bool pt;
+        if (flags) {
+            pt = (flags[i] & 2u) != 0;  // PopulationRecord::pub_transport as given
+        } else {
+            pt = bern(u[1], plan.thr_pt) && working && pt_users < plan.transport_points;
+            if (pt) ++pt_users;
+        }
         r.flags = pt ? EPI_F_PUBLIC_TRANSPORT : 0;
         r.home_x = h.x0; r.home_y = h.y0;
         if (working) {
@@ -306,7 +390,9 @@ int build_world(const epi_params& p, std::vector<epi_agent_record>& out, epi_geo
             if (bern(u[2], plan.thr_staff)) { r.work_status = EPI_WS_HOSPITAL_STAFF; r.work_start_at = 8; }
             else r.work_status = EPI_WS_NORMAL;
         } else {
-            r.work_x = h.x0; r.work_y = h.y0;
+            // Auto: create_citizen keeps the house; Csv: from_record keeps the cycled office
+            r.work_x = flags ? o.x0 : h.x0;
+            r.work_y = flags ? o.y0 : h.y0;
             r.work_status = EPI_WS_NA;
         }
         r.immunity = (int8_t)((int32_t)uniform_index(u[3], 5u) - 2);

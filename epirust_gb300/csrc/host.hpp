@@ -23,7 +23,10 @@ epi_area office_area(const epi_geography& g, uint32_t k);
 
 // Epidemiology::new world build on the host (geography, population, starting infections,
 // start points, hospital resize, essential workers).  Returns EPI_OK or an error code.
-int build_world(const epi_params& p, std::vector<epi_agent_record>& out, epi_geography& geo, std::string& err);
+// flags (Csv population, bit 0 working, bit 1 public transport) replace the Auto draws.
+int build_world(const epi_params& p, std::vector<epi_agent_record>& out, epi_geography& geo, std::string& err,
+                const uint8_t* flags = nullptr);
+int read_population_csv(const std::string& path, std::vector<uint8_t>& flags, std::string& err);
 
 // Everything about a world build that is not per agent: the checks of generate_population
 // and set_starting_infections, the Bernoulli thresholds, the public-transport budget of
@@ -37,8 +40,9 @@ struct WorldPlan {
     uint32_t key0 = 0, key1 = 0;
     struct Infection { uint32_t agent; uint8_t state; uint32_t day; };
     std::vector<Infection> infections;
+    const uint8_t* flags = nullptr;  // Csv population flags (not owned)
 };
-int world_plan(const epi_params& p, WorldPlan& plan, std::string& err);
+int world_plan(const epi_params& p, WorldPlan& plan, std::string& err, const uint8_t* flags = nullptr);
 
 struct Report {
     uint32_t hour;

@@ -23,17 +23,20 @@ struct WorldDev {
     int32_t hx0, hy0, ox0, oy0;  // housing and work-area origins
     uint32_t key0, key1;
     uint32_t transport_points;
+    uint32_t csv;  // 1: working and public transport come from the population flags
     uint64_t thr_work, thr_pt, thr_staff, thr_ess;
 };
 
 // Citizens of every world (one 256-agent chunk per block iteration).  elig[slot] = 1 for
 // agents that would take public transport if the budget allowed; chunk_elig[c] counts them.
+// flags[slot] (bit 0 working, bit 1 public transport) replace the draws of Csv worlds.
 __global__ void __launch_bounds__(kThreads) k_world_citizens(const WorldDev* __restrict__ W,
                                                              const uint32_t* __restrict__ chunk_rep, uint32_t n_chunks,
                                                              uint32_t* __restrict__ pos, uint2* __restrict__ st,
                                                              uint32_t* __restrict__ home, uint32_t* __restrict__ work,
                                                              uint32_t* __restrict__ wsa, uint32_t* __restrict__ elig,
-                                                             uint32_t* __restrict__ chunk_elig) {
+                                                             uint32_t* __restrict__ chunk_elig,
+                                                             const uint8_t* __restrict__ flags) {
     for (uint32_t c = blockIdx.x; c < n_chunks; c += gridDim.x) {
         const WorldDev& w = W[chunk_rep ? chunk_rep[c] : 0u];
         const uint32_t slot = c * kChunk + threadIdx.x;
@@ -42,12 +45,14 @@ __global__ void __launch_bounds__(kThreads) k_world_citizens(const WorldDev* __r
         if (i < w.n) {
             uint32_t u[4];
             philox4x32(i, kWorldHour, kBlkCitizen, 0u, w.key0, w.key1, u);
-            const bool working = (uint64_t)u[0] < w.thr_work;
+            const uint32_t fl = w.csv ? flags[slot] : 0u;
+            const bool working = w.csv ? (fl & 1u) != 0u : (uint64_t)u[0] < w.thr_work;
             const uint32_t house = i % w.houses, office = i % w.offices;
             const int32_t hx = w.hx0 + 2 * (int32_t)(house % w.houses_x), hy = w.hy0 + 2 * (int32_t)(house / w.houses_x);
             const int32_t ox = w.ox0 + 10 * (int32_t)(office % w.offices_x), oy = w.oy0 + 10 * (int32_t)(office / w.offices_x);
-            e = working && (uint64_t)u[1] < w.thr_pt;
-            uint32_t ws = EPI_WS_NA, start = 0u, wk = pack_xy(hx, hy);
+            e = !w.csv && working && (uint64_t)u[1] < w.thr_pt;
+            // Auto: a non-worker's work area is its house; Csv (from_record): the cycled office
+            uint32_t ws = EPI_WS_NA, start = 0u, wk = w.csv ? pack_xy(ox, oy) : pack_xy(hx, hy);
             if (working) {
                 wk = pack_xy(ox, oy);
                 if ((uint64_t)u[2] < w.thr_staff) {
@@ -73,7 +78,9 @@ __global__ void __launch_bounds__(kThreads) k_world_citizens(const WorldDev* __r
             home[slot] = pack_xy(hx, hy);
             work[slot] = wk;
             wsa[slot] = start;
-            st[slot] = make_uint2((uint32_t)EPI_S | (kHome << kAreaShift) | (ws << kWsShift) | (imm << kImmShift), 0u);
+            st[slot] = make_uint2((uint32_t)EPI_S | (kHome << kAreaShift) | (ws << kWsShift) | (imm << kImmShift) |
+                                      ((fl & 2u) ? kPt : 0u),
+                                  0u);
         }
         elig[slot] = e ? 1u : 0u;
         const int cnt = __syncthreads_count(e);

@@ -81,12 +81,26 @@ def define_geography(grid_size: int) -> EpiGeography:
     return g
 
 
+def read_population_csv(path: str) -> np.ndarray:
+    """Population::Csv rows as flags (bit 0 working, bit 1 public transport)."""
+    n = C.c_uint32(0)
+    check(lib().epi_population_read_csv(os.fsencode(path), None, 0, C.byref(n)))
+    flags = np.zeros(n.value, dtype=np.uint8)
+    check(lib().epi_population_read_csv(os.fsencode(path), flags.ctypes.data, n.value, C.byref(n)))
+    return flags
+
+
 def world_build(params: EpiParams) -> tuple[np.ndarray, EpiGeography]:
     """Host world build (population, start points, hospital) as agent records."""
     n = params.number_of_agents
     recs = np.zeros(n, dtype=AGENT_DTYPE)
     g = EpiGeography()
-    check(lib().epi_world_build(C.byref(params), recs.ctypes.data, n, C.byref(g)))
+    if params.population_source == 1:
+        flags = read_population_csv(params.population_file.decode())
+        check(lib().epi_world_build_population(C.byref(params), flags.ctypes.data, len(flags), recs.ctypes.data,
+                                               C.byref(g)))
+    else:
+        check(lib().epi_world_build(C.byref(params), recs.ctypes.data, n, C.byref(g)))
     return recs, g
 
 
@@ -99,7 +113,11 @@ class Epidemiology:
         if seed is not None:
             self.params.seed = seed
         h = C.c_void_p()
-        if records is None:
+        if records is None and self.params.population_source == 1:  # Population::Csv
+            flags = read_population_csv(self.params.population_file.decode())
+            self.params.number_of_agents = len(flags)
+            rc = lib().epi_engine_create_population(C.byref(self.params), flags.ctypes.data, len(flags), C.byref(h))
+        elif records is None:
             rc = lib().epi_engine_create(C.byref(self.params), C.byref(h))
         else:
             records = np.ascontiguousarray(records, dtype=AGENT_DTYPE)

@@ -120,6 +120,11 @@ typedef struct {
     double hospital_occupancy_trigger;
     /* extension: counter-based random stream key (the reference RNG is unseeded) */
     uint64_t seed;
+    /* Population source: 0 Auto (number_of_agents and the two percentages), 1 Csv (one row
+     * per agent, common/src/config/population.rs:31-34; the rows come with
+     * epi_engine_create_population and number_of_agents is their count). */
+    uint32_t population_source;
+    char population_file[256];  /* Csv: the "file" of the config (NUL-terminated) */
 } epi_params;
 
 /* Per-agent snapshot (host layout, used for oracle comparison and checkpoints).
@@ -170,6 +175,18 @@ int epi_geography_increase_hospital_size(epi_geography* geo, uint32_t grid_size)
  * (common/src/disease/mod.rs:88-99). */
 double epi_disease_transmission_rate(const epi_params* p, uint32_t infection_day);
 int epi_disease_is_to_be_hospitalized(const epi_params* p, uint32_t infection_day);
+
+/* Csv population (grid.rs:194-231, citizen/population_record.rs): read the columns
+ * "working" and "pub_transport" ("True" / "False") of every row into flags (bit 0 working,
+ * bit 1 public transport).  flags may be NULL to count the rows; at most cap are written. */
+int epi_population_read_csv(const char* path, uint8_t* flags, uint32_t cap, uint32_t* n);
+/* World build / engine from per-agent population flags (n == params->number_of_agents):
+ * agent i gets house i mod houses and office i mod offices (the cycled iterators of
+ * read_population), working and public transport from its flags, and the rest as in the
+ * Auto build (Citizen::from_record, citizen/mod.rs:155-180). */
+int epi_world_build_population(const epi_params* params, const uint8_t* flags, uint32_t n, epi_agent_record* out,
+                               epi_geography* geo);
+int epi_engine_create_population(const epi_params* params, const uint8_t* flags, uint32_t n, epi_engine** out);
 
 /* World build of Epidemiology::new (engine/src/epidemiology_simulation.rs:85-117):
  * geography, Auto population, starting infections, hospital resize and essential

@@ -295,7 +295,11 @@ void o_import_citizen(const epi_agent_record* r, uint32_t id, citizen* c, pt* po
     c->ws = r->work_status;
     c->work_start_at = r->work_start_at;
     c->home = mk_area(r->home_x, r->home_y, r->home_x + 1, r->home_y + 1);
-    c->work = c->ws == EPI_WS_NA ? c->home : mk_area(r->work_x, r->work_y, r->work_x + 9, r->work_y + 9);
+    /* a non-worker keeps the work area it was built with: its house (Auto, create_citizen)
+       or the cycled office (Csv, Citizen::from_record) */
+    c->work = (c->ws == EPI_WS_NA && r->work_x == r->home_x && r->work_y == r->home_y)
+                  ? c->home
+                  : mk_area(r->work_x, r->work_y, r->work_x + 9, r->work_y + 9);
     c->current = mk_area(r->area_x0, r->area_y0, r->area_x1, r->area_y1);
 }
 

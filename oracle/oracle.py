@@ -44,6 +44,7 @@ class Params(C.Structure):
         ("spread_rate_threshold", C.c_uint32), ("n_vaccinations", C.c_int32),
         ("vaccination_at_hour", C.c_uint32 * MAX_VACC), ("vaccination_percent", C.c_double * MAX_VACC),
         ("hospital_occupancy_trigger", C.c_double), ("seed", C.c_uint64),
+        ("population_source", C.c_uint32), ("population_file", C.c_char * 256),
     ]
 
 

@@ -81,8 +81,8 @@ def test_config_defaults_and_errors(engine_built):
     del cfg["starting_infections"]
     assert Config(json.dumps(cfg)).params.exposed == 1  # StartingInfections::default
     bad = make_config()
-    bad["population"] = {"Csv": {"file": "x.csv", "cols": []}}
-    with pytest.raises(EpiError, match="Csv"):
+    bad["population"] = {"Csv": {"file": "/nonexistent/x.csv", "cols": []}}
+    with pytest.raises(EpiError, match="population file"):
         Config(json.dumps(bad))
     bad = make_config()
     del bad["disease"]
