@@ -190,7 +190,7 @@ __global__ void __launch_bounds__(kThreads) k_decide(const DevParams* __restrict
             // The claim goes out before the infection update so that its round trip overlaps it.
             const uint32_t key = claim_key(hour, i);
             const uint32_t old = moving ? atomicMin(&rclaim[(size_t)nc.y * P.W + nc.x], key) : kNoClaim;
-            if (infect) infection_dynamics(P, pl, s, at, area_rect(P, st_area(s), hm, wk), nc, hour, dr);
+            if (infect) infection_dynamics(P, pl, s, at, hm, wk, nc, hour, dr);
             if (moving) {
                 // The claim that atomicMin finds names an agent this one competes with: of
                 // the two the higher index loses.  Every claimant but the cell's lowest is
@@ -239,6 +239,11 @@ __global__ void __launch_bounds__(kThreads) k_commit(const DevParams* __restrict
                                                      const uint32_t* __restrict__ prev) {
     const uint32_t hour = *hour_base + hour_offset;
     const uint32_t base = blockIdx.x * (blockDim.x * S) + threadIdx.x;
+    // a single world's parameters once per thread; an ensemble looks each slot's replicate up
+    const bool one = chunk_rep == nullptr;
+    const uint32_t active0 = one ? Pall[0].active : 0u, off0 = one ? Pall[0].agent_off : 0u;
+    const uint32_t wp0 = one ? (uint32_t)Pall[0].WP : 0u;
+    const bool ended0 = one && run_ended(prev, 0u);
     uint32_t t[S], p[S], l[S];
 #pragma unroll
     for (int k = 0; k < S; ++k) {
@@ -247,33 +252,38 @@ __global__ void __launch_bounds__(kThreads) k_commit(const DevParams* __restrict
         p[k] = slot < n_slots ? pos[slot] : 0u;
         l[k] = lost && slot < n_slots ? lost[slot] : 0u;
     }
-    const DevParams* Pr[S];
-    uint32_t won[S], rr[S];
-#pragma unroll
-    for (int k = 0; k < S; ++k) {
-        const uint32_t slot = base + k * blockDim.x;
-        rr[k] = chunk_rep && t[k] != kNoAction ? chunk_rep[slot / kChunk] : 0u;
-        Pr[k] = Pall + rr[k];
-        won[k] = kNoClaim;  // never equal to a key: stays put
-        if (t[k] != kNoAction && target_xy(t[k]) != p[k]) {
-            const uint32_t xy = target_xy(t[k]);
-            if (lost) won[k] = l[k] == hour ? kNoClaim : claim_key(hour, slot - Pr[k]->agent_off);
-            else won[k] = claim[Pr[k]->claim_off + (size_t)unpack_y(xy) * (uint32_t)Pr[k]->W + unpack_x(xy)];
-        }
-    }
 #pragma unroll
     for (int k = 0; k < S; ++k) {
         if (t[k] == kNoAction) continue;
-        const DevParams& P = *Pr[k];
-        if (!P.active || run_ended(prev, rr[k])) continue;
         const uint32_t slot = base + k * blockDim.x;
-        const uint32_t i = slot - P.agent_off;
-        const uint32_t WP = (uint32_t)P.WP;
-        uint8_t* rplane = plane + P.plane_off;
+        uint32_t r = 0u, active = active0, off = off0, WP = wp0;
+        uint64_t plane_off = 0u;
+        bool ended = ended0;
+        if (!one) {
+            r = chunk_rep[slot / kChunk];
+            const DevParams& P = Pall[r];
+            active = P.active;
+            off = P.agent_off;
+            WP = (uint32_t)P.WP;
+            plane_off = P.plane_off;
+            ended = run_ended(prev, r);
+        }
+        if (!active || ended) continue;
         const uint32_t xy = target_xy(t[k]), cls = target_class(t[k]), cls0 = target_old_class(t[k]);
+        bool win = false;
+        if (xy != p[k]) {
+            if (lost) {
+                win = l[k] != hour;
+            } else {
+                const DevParams& P = Pall[r];
+                win = claim[P.claim_off + (size_t)unpack_y(xy) * (uint32_t)P.W + unpack_x(xy)] ==
+                      claim_key(hour, slot - off);
+            }
+        }
+        uint8_t* rplane = plane + plane_off;
         const size_t old_cell = (size_t)(unpack_y(p[k]) + 1) * WP + (unpack_x(p[k]) + 1);
         size_t new_cell = old_cell;
-        if (won[k] == claim_key(hour, i)) {
+        if (win) {
             new_cell = (size_t)(unpack_y(xy) + 1) * WP + (unpack_x(xy) + 1);
             rplane[old_cell] = 0;
             rplane[new_cell] = (uint8_t)cls;
@@ -285,7 +295,7 @@ __global__ void __launch_bounds__(kThreads) k_commit(const DevParams* __restrict
         // being infectious (rare: a few agents per hour)
         const bool inf0 = cls0 >= 2u, inf1 = cls >= 2u;
         if (danger && (inf0 || inf1) && (inf0 != inf1 || new_cell != old_cell)) {
-            uint8_t* rd = danger + P.plane_off;
+            uint8_t* rd = danger + plane_off;
             if (inf0) danger_add(rd, old_cell, WP, -1);
             if (inf1) danger_add(rd, new_cell, WP, +1);
         }

@@ -217,8 +217,10 @@ __device__ __forceinline__ Cell goto_area(const PlaneView& pl, uint32_t s, const
 
 // DiseaseStateMachine::next with the default DiseaseHandler (ddh:41-86) for the hour's
 // proposed cell; at is the Exposed/Pre at_hour word.
+// (The agent's current area, needed only when an infectious neighbour exists, is decoded from
+// its code and home / work corners here rather than by the caller.)
 __device__ __forceinline__ void infection_dynamics(const DevParams& P, const PlaneView& pl, uint32_t& s, uint32_t& at,
-                                                   const Rect& cur, Cell cell, uint32_t hour, Draws& dr) {
+                                                   uint32_t home, uint32_t work, Cell cell, uint32_t hour, Draws& dr) {
     const uint32_t v = s & kStateMask;
     if (v == EPI_S) {
         if (s & (kWq | kVacc)) return;
@@ -226,6 +228,7 @@ __device__ __forceinline__ void infection_dynamics(const DevParams& P, const Pla
         if (pl.danger && pl.danger_at(cell.x, cell.y) == 0u) return;
         const Rows3 rows = rows_around(pl, cell.x, cell.y);
         if (!any_infectious(rows)) return;
+        const Rect cur = area_rect(P, st_area(s), home, work);
         const uint32_t cand = valid_neighbours(cur, pl.G, cell.x, cell.y) & infectious_mask(rows);
         if (!cand) return;
         const uint32_t high = high_mask(rows);
