@@ -34,8 +34,10 @@ sys.path.insert(0, ROOT)
 DEFAULT_CONFIG = os.path.join(ROOT, "tests", "golden", "c2_small_pox_1m.json")
 METRIC = "agent-hours/s"
 # Algorithmic bytes of one k_decide launch per agent: pos 4 + st 8 + home 4 + work 4 read,
-# st 8 + tgt 4 written; plus one read of the (G+1)^2 byte occupancy plane.
+# st 8 + tgt 4 written; plus one read of the (G+1)^2 byte occupancy plane and of the
+# (G+1)^2 infectious-neighbour counts.
 DECIDE_BYTES_PER_AGENT = 32
+DECIDE_PLANES = 2
 
 
 def _peaks():
@@ -377,7 +379,7 @@ def run_gpu(args, cfg):
     total_kernel_ms = sum(ms for _, ms in stats.values())
     launches_d, ms_d = stats["k_decide"]
     avg_ms = ms_d / max(launches_d, 1)
-    alg_bytes = DECIDE_BYTES_PER_AGENT * n + cells
+    alg_bytes = DECIDE_BYTES_PER_AGENT * n + DECIDE_PLANES * cells
     achieved = alg_bytes / (avg_ms / 1000.0) / 1e9
     peak, peak_kind = _peaks()
     # issue roofline: warp instructions per k_decide launch (committed ncu launch list, scaled

@@ -1472,18 +1472,19 @@ size_t epi_abi_struct_size(const char* name) {
 }
 
 // Algorithmic bytes of one hour over all replicates (the roofline numerator): the agent
-// words the hour's kernels must read and write plus one pass over each occupancy plane.
+// words the hour's kernels must read and write plus one pass over each plane.
 //   movement hours and hours 0/23: decide reads pos 4 + st 8 + home 4 + work 4, writes st 8 +
-//   tgt 4; commit reads tgt 4 + pos 4, writes pos 4; plane (G+1)^2 bytes read once.
-//   sleep hours: st.x read 4 (+ write 4 on the first sleep hour).
+//   tgt 4; commit reads tgt 4 + pos 4 + lost 4, writes pos 4; the occupancy plane and the
+//   infectious-neighbour counts, (G+1)^2 bytes each, read once.
+//   hour 1: st.x read 4 + write 4; hours 2-6 of a segment move no data.
 int epi_engine_hour_bytes(const epi_engine* h, uint32_t hour, double* bytes) {
     if (!h || !bytes) return EPI_ERR_ARG;
     const uint32_t hod = hour % 24u;
     double b = 0.0;
     for (const auto& rep : h->reps) {
         const double n = (double)rep.n, side = (double)rep.p.grid_size + 1.0;
-        if (hod >= 1u && hod <= 6u) b += n * (hod == 1u ? 8.0 : 4.0);
-        else b += n * 44.0 + side * side;
+        if (hod >= 1u && hod <= 6u) b += hod == 1u ? n * 8.0 : 0.0;
+        else b += n * 48.0 + 2.0 * side * side;
     }
     *bytes = b;
     return EPI_OK;
