@@ -264,11 +264,10 @@ def run_surrogate(args) -> dict:
     agents with 8 replicates each, the same ABM budget on unscreened candidates)."""
     from epirust_gb300.sweep import screened_sweep, train_on_abm
 
-    nets, train = train_on_abm(runs=args.train_runs, held_out=args.train_runs // 8, steps=args.train_steps)
+    net, train = train_on_abm(runs=args.train_runs, held_out=args.train_runs // 8, steps=args.train_steps)
     train.pop("curves")
-    sweep = screened_sweep(nets, keep=args.sweep_keep, replicates=args.sweep_replicates)
-    for n in nets:
-        n.close()
+    sweep = screened_sweep(net, keep=args.sweep_keep, replicates=args.sweep_replicates)
+    net.close()
     sweep["note"] = ("abm_only_sweep_s_estimated = every candidate x replicates through the ABM at the rate "
                      "measured for the re-run stage")
     return {"metric": "surrogate sweep speedup @<=5% peak err", "training": train, "sweep": sweep}

@@ -119,7 +119,7 @@ class LaunchShape(C.Structure):
 MLP_EXPORTS = [
     "epi_mlp_create", "epi_mlp_destroy", "epi_mlp_last_error", "epi_mlp_set_stream", "epi_mlp_param_count",
     "epi_mlp_get_params", "epi_mlp_set_params", "epi_mlp_set_dataset", "epi_mlp_train", "epi_mlp_gradients",
-    "epi_mlp_predict", "epi_mlp_score", "epi_mlp_kernels_launched",
+    "epi_mlp_predict", "epi_mlp_score", "epi_mlp_kernels_launched", "epi_mlp_members",
 ]
 
 
@@ -127,7 +127,7 @@ class MlpConfig(C.Structure):
     _fields_ = [
         ("in_dim", C.c_uint32), ("hidden", C.c_uint32), ("hidden_layers", C.c_uint32), ("out_dim", C.c_uint32),
         ("batch", C.c_uint32), ("lr", C.c_float), ("beta1", C.c_float), ("beta2", C.c_float), ("eps", C.c_float),
-        ("seed", C.c_uint64),
+        ("members", C.c_uint32), ("seed", C.c_uint64),
     ]
 
 _lib = None
@@ -227,6 +227,7 @@ def lib():
     _sig(L, "epi_mlp_predict", C.c_int, [V, F, C.c_uint32, F])
     _sig(L, "epi_mlp_score", C.c_int, [V, F, C.c_uint32, F, F])
     _sig(L, "epi_mlp_kernels_launched", C.c_int, [V, P(C.c_uint64)])
+    _sig(L, "epi_mlp_members", C.c_int, [V, P(C.c_uint32)])
     _lib = L
     return L
 

@@ -34,6 +34,8 @@ enum Epilogue : int {
     kEpDw = 3       // outf = acc (fp32)
 };
 
+// Pointers are those of member 0 of a stack of networks; member m (blockIdx.z) adds m times
+// the ms_* element stride of each (0: shared by all members).
 struct EpiArgs {
     const float* bias = nullptr;        // [N]
     float* z = nullptr;                 // [M x N]
@@ -48,7 +50,23 @@ struct EpiArgs {
     uint32_t n_valid = 0;               // real output columns
     uint32_t m_valid = 0;               // real sample rows
     float grad_scale = 0.f;
+    uint64_t ms_bias = 0, ms_z = 0, ms_zin = 0, ms_out = 0, ms_outf = 0, ms_target = 0, ms_score = 0, ms_loss = 0;
 };
+
+// The member-m view of a.
+__device__ __forceinline__ EpiArgs member_args(const EpiArgs& a, uint32_t m) {
+    EpiArgs b = a;
+    if (b.bias) b.bias += m * a.ms_bias;
+    if (b.z) b.z += m * a.ms_z;
+    if (b.zin) b.zin += m * a.ms_zin;
+    if (b.out) b.out += m * a.ms_out;
+    if (b.out_t) b.out_t += m * a.ms_out;  // both orientations hold M x N elements
+    if (b.outf) b.outf += m * a.ms_outf;
+    if (b.target) b.target += m * a.ms_target;
+    if (b.score) b.score += m * a.ms_score;
+    if (b.loss) b.loss += m * a.ms_loss;
+    return b;
+}
 
 __device__ __forceinline__ uint32_t smem_u32(const void* p) { return (uint32_t)__cvta_generic_to_shared(p); }
 
@@ -77,11 +95,13 @@ __device__ __forceinline__ bool mbar_wait(uint64_t* bar, uint32_t parity) {
     return false;
 }
 
-__device__ __forceinline__ void tma_load_2d(void* dst, const CUtensorMap* map, int32_t x, int32_t y, uint64_t* bar) {
+// Tile (x, y) of member z of a 3-D tensor map {K, rows, members}.
+__device__ __forceinline__ void tma_load_3d(void* dst, const CUtensorMap* map, int32_t x, int32_t y, int32_t z,
+                                            uint64_t* bar) {
     asm volatile(
-        "cp.async.bulk.tensor.2d.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1, {%2, %3}], [%4];" ::"r"(
+        "cp.async.bulk.tensor.3d.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1, {%2, %3, %4}], [%5];" ::"r"(
             smem_u32(dst)),
-        "l"(reinterpret_cast<uint64_t>(map)), "r"(x), "r"(y), "r"(smem_u32(bar))
+        "l"(reinterpret_cast<uint64_t>(map)), "r"(x), "r"(y), "r"(z), "r"(smem_u32(bar))
         : "memory");
 }
 
@@ -219,11 +239,13 @@ constexpr uint32_t gemm_smem_bytes() {
     return (uint32_t)kStages * (uint32_t)(kBM + BN) * kBK * 2u + 1024u + 16384u;
 }
 
-// Grid (M / 128, N / BN); M % 128 == 0, N % BN == 0, K % 64 == 0 (checked by the host).
+// Grid (M / 128, N / BN, members); M % 128 == 0, N % BN == 0, K % 64 == 0 (checked by the
+// host).  za / zb: 1 when A / B differ per member, 0 when the member stack shares member 0's.
 template <int BN, int EP>
 __global__ void __launch_bounds__(kGemmThreads, 1)
     k_gemm(const __grid_constant__ CUtensorMap ta, const __grid_constant__ CUtensorMap tb, uint32_t M, uint32_t N,
-           uint32_t K, EpiArgs args, int* err) {
+           uint32_t K, EpiArgs margs, uint32_t za, uint32_t zb, int* err) {
+    const EpiArgs args = member_args(margs, blockIdx.z);
     static_assert(BN == 64 || BN == 128 || BN == 256, "UMMA N");
     constexpr uint32_t kABytes = kBM * kBK * 2, kBBytes = BN * kBK * 2, kStageBytes = kABytes + kBBytes;
     extern __shared__ uint8_t smem_raw[];
@@ -265,8 +287,8 @@ __global__ void __launch_bounds__(kGemmThreads, 1)
             const uint32_t s = kb % kStages;
             uint8_t* sa = smem + s * kStageBytes;
             mbar_expect_tx(&full_bar[s], kStageBytes);
-            tma_load_2d(sa, &ta, (int32_t)(kb * kBK), (int32_t)m0, &full_bar[s]);
-            tma_load_2d(sa + kABytes, &tb, (int32_t)(kb * kBK), (int32_t)n0, &full_bar[s]);
+            tma_load_3d(sa, &ta, (int32_t)(kb * kBK), (int32_t)m0, (int32_t)(blockIdx.z * za), &full_bar[s]);
+            tma_load_3d(sa + kABytes, &tb, (int32_t)(kb * kBK), (int32_t)n0, (int32_t)(blockIdx.z * zb), &full_bar[s]);
             ++issued;
         };
         for (uint32_t kb = 0; kb < nk && kb < (uint32_t)kStages; ++kb) load_stage(kb);

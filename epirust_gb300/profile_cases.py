@@ -4,11 +4,11 @@ package and exits.
     python -m epirust_gb300.profile_cases tick --agents 1000000 --grid 2500 --hours 48
         the config-2 world (tests/golden/c2_small_pox_1m.json) resized, hours 1..hours-1
         through simulate_hours (one CUDA graph per call); --events adds CUDA events per kernel
-    python -m epirust_gb300.profile_cases mlp-train --steps 30
-        the surrogate network 8 -> 512 x 3 -> 600, batch 256, on a seeded synthetic set of
-        4,096 samples: `steps` Adam steps (one graph replay each)
-    python -m epirust_gb300.profile_cases mlp-screen --candidates 65536
-        one network scoring `candidates` parameter vectors against a curve
+    python -m epirust_gb300.profile_cases mlp-train --steps 30 [--members M]
+        the surrogate network 8 -> 512 x 3 -> 600 (M members in one handle), batch 256, on a
+        seeded synthetic set of 4,096 samples: `steps` Adam steps (one graph replay each)
+    python -m epirust_gb300.profile_cases mlp-screen --candidates 65536 [--members M]
+        the network (M members) scoring `candidates` parameter vectors against a curve
 """
 from __future__ import annotations
 
@@ -42,29 +42,29 @@ def tick(args) -> dict:
     return out
 
 
-def _net():
+def _net(members: int = 1):
     from .surrogate import Surrogate
 
-    return Surrogate(in_dim=8, out_dim=600, hidden=512, hidden_layers=3, batch=256, seed=1)
+    return Surrogate(in_dim=8, out_dim=600, hidden=512, hidden_layers=3, batch=256, seed=1, members=members)
 
 
 def mlp_train(args) -> dict:
     rng = np.random.default_rng(0)
     x = rng.random((4096, 8))
     y = np.sin(x @ rng.normal(size=(8, 600))) * 0.5
-    net = _net()
+    net = _net(args.members)
     net.set_dataset(x, y)
     t0 = time.perf_counter()
-    losses = net.train(args.steps, seed=0)
+    losses = np.atleast_2d(net.train(args.steps, seed=0))
     dt = time.perf_counter() - t0
     net.close()
-    return {"steps": args.steps, "s": dt, "ms_per_step": 1000 * dt / max(args.steps, 1),
-            "first_loss": float(losses[0]), "last_loss": float(losses[-1])}
+    return {"steps": args.steps, "members": args.members, "s": dt, "ms_per_step": 1000 * dt / max(args.steps, 1),
+            "first_loss": float(losses[:, 0].mean()), "last_loss": float(losses[:, -1].mean())}
 
 
 def mlp_screen(args) -> dict:
     rng = np.random.default_rng(1)
-    net = _net()
+    net = _net(args.members)
     cand = rng.random((args.candidates, 8))
     target = rng.random(600)
     net.score(cand[:1024], target)  # warm-up (buffers, tensor maps)
@@ -85,8 +85,10 @@ def main() -> None:
     t.add_argument("--events", action="store_true")
     m = sub.add_parser("mlp-train")
     m.add_argument("--steps", type=int, default=30)
+    m.add_argument("--members", type=int, default=1)
     s = sub.add_parser("mlp-screen")
     s.add_argument("--candidates", type=int, default=65536)
+    s.add_argument("--members", type=int, default=1)
     args = ap.parse_args()
     fn = {"tick": tick, "mlp-train": mlp_train, "mlp-screen": mlp_screen}[args.case]
     print(json.dumps(fn(args)))

@@ -1,7 +1,8 @@
 """The learned surrogate and the parameter sweeps it screens.
 
-`Surrogate` wraps one MLP of include/epi_surrogate.h (trained and evaluated by the sm_103a
-kernels; there is no CPU path).  The rest is host orchestration:
+`Surrogate` wraps one handle of include/epi_surrogate.h -- an ensemble of `members` MLPs of
+one shape, trained and evaluated together by the sm_103a kernels (there is no CPU path).
+The rest is host orchestration:
 
 * `PARAMS`: the eight sweep parameters and their ranges (regular and high transmission rate,
   death rate, lockdown threshold, essential-worker fraction, vaccination hour and fraction,
@@ -139,12 +140,16 @@ def peak_height(curves: np.ndarray, days: int) -> np.ndarray:
 
 
 class Surrogate:
-    """One MLP on the GPU (epi_mlp_*): in_dim -> hidden x hidden_layers (GELU) -> out_dim."""
+    """`members` MLPs on the GPU (epi_mlp_*): in_dim -> hidden x hidden_layers (GELU) -> out_dim.
+    Member m is initialised from seed + m and trained on minibatches shuffled from
+    train(seed=s) + m: it equals a one-member Surrogate built and trained with those seeds.
+    predict() and score() give the ensemble mean; the *_members variants every member's."""
 
     def __init__(self, in_dim: int = 8, out_dim: int = 600, hidden: int = 512, hidden_layers: int = 3,
                  batch: int = 256, lr: float = 1e-3, seed: int = 0, beta1: float = 0.9, beta2: float = 0.999,
-                 eps: float = 1e-8):
-        self.cfg = MlpConfig(in_dim, hidden, hidden_layers, out_dim, batch, lr, beta1, beta2, eps, seed)
+                 eps: float = 1e-8, members: int = 1):
+        self.members = int(members)
+        self.cfg = MlpConfig(in_dim, hidden, hidden_layers, out_dim, batch, lr, beta1, beta2, eps, self.members, seed)
         h = C.c_void_p()
         rc = lib().epi_mlp_create(C.byref(self.cfg), C.byref(h))
         if rc != _lib.EPI_OK:
@@ -181,14 +186,19 @@ class Surrogate:
     def _ptr(a: np.ndarray):
         return a.ctypes.data_as(C.POINTER(C.c_float))
 
+    def _shape(self, a: np.ndarray) -> np.ndarray:
+        """(members, ...) -> (...) for a one-member handle."""
+        return a[0] if self.members == 1 else a
+
     def get_params(self) -> np.ndarray:
-        out = np.zeros(self.n_params, dtype=np.float32)
+        """(n_params,) for one member, else (members, n_params)."""
+        out = np.zeros((self.members, self.n_params), dtype=np.float32)
         self._check(lib().epi_mlp_get_params(self._h, self._ptr(out)))
-        return out
+        return self._shape(out)
 
     def set_params(self, flat) -> None:
         a = self._f32(flat)
-        assert a.size == self.n_params
+        assert a.size == self.members * self.n_params
         self._check(lib().epi_mlp_set_params(self._h, self._ptr(a)))
 
     def set_output_scaling(self, mean, scale) -> None:
@@ -215,31 +225,46 @@ class Surrogate:
         self._check(lib().epi_mlp_set_dataset(self._h, self._ptr(x), self._ptr(y), x.shape[0]))
 
     def train(self, steps: int, seed: int = 0) -> np.ndarray:
-        losses = np.zeros(max(steps, 1), dtype=np.float32)
+        """Per-step losses: (steps,) for one member, else (members, steps)."""
+        losses = np.zeros((self.members, max(steps, 1)), dtype=np.float32)
         self._check(lib().epi_mlp_train(self._h, steps, seed, self._ptr(losses)))
-        return losses[:steps]
+        return self._shape(losses[:, :steps])
 
-    def gradients(self, x, y) -> tuple[float, np.ndarray]:
+    def gradients(self, x, y):
+        """Loss and gradients of one minibatch: (float, (n_params,)) for one member, else
+        ((members,), (members, n_params))."""
         x, y = self._f32(x), self._f32(y)
-        g = np.zeros(self.n_params, dtype=np.float32)
-        loss = C.c_float(0.0)
+        g = np.zeros((self.members, self.n_params), dtype=np.float32)
+        loss = np.zeros(self.members, dtype=np.float32)
         self._check(lib().epi_mlp_gradients(self._h, self._ptr(x), self._ptr(y), x.shape[0], self._ptr(g),
-                                            C.byref(loss)))
-        return loss.value, g
+                                            self._ptr(loss)))
+        return (float(loss[0]), g[0]) if self.members == 1 else (loss, g)
 
-    def predict(self, x) -> np.ndarray:
+    def predict_members(self, x) -> np.ndarray:
+        """Every member's curves: (members, n, out_dim)."""
         x = self._f32(x)
-        y = np.zeros((x.shape[0], self.cfg.out_dim), dtype=np.float32)
+        y = np.zeros((self.members, x.shape[0], self.cfg.out_dim), dtype=np.float32)
         self._check(lib().epi_mlp_predict(self._h, self._ptr(x), x.shape[0], self._ptr(y)))
         return self._from_z(y)
 
-    def score(self, x, target) -> np.ndarray:
-        """Squared distance to the target, summed over outputs, in the training scale (the
-        standardised outputs when set_output_scaling was called)."""
+    def predict(self, x) -> np.ndarray:
+        """The ensemble-mean curves (n, out_dim)."""
+        y = self.predict_members(x)
+        return y[0] if self.members == 1 else y.mean(axis=0, dtype=np.float64).astype(np.float32)
+
+    def score_members(self, x, target) -> np.ndarray:
+        """Squared distance of every member's curves to the target, summed over outputs, in the
+        training scale (the standardised outputs when set_output_scaling was called):
+        (members, n)."""
         x, t = self._f32(x), self._to_z(np.asarray(target)[None])[0]
-        s = np.zeros(x.shape[0], dtype=np.float32)
+        s = np.zeros((self.members, x.shape[0]), dtype=np.float32)
         self._check(lib().epi_mlp_score(self._h, self._ptr(x), x.shape[0], self._ptr(t), self._ptr(s)))
         return s
+
+    def score(self, x, target) -> np.ndarray:
+        """The members' mean score_members (n,)."""
+        s = self.score_members(x, target)
+        return s[0] if self.members == 1 else s.mean(axis=0)
 
     def kernels_launched(self) -> int:
         v = C.c_uint64(0)
@@ -247,14 +272,16 @@ class Surrogate:
         return v.value
 
 
-def screen(members: list[Surrogate], candidates: np.ndarray, target: np.ndarray, keep: int, days: int,
-           peak_tolerance: float = 0.05):
+def screen(nets, candidates: np.ndarray, target: np.ndarray, keep: int, days: int, peak_tolerance: float = 0.05):
     """Rank candidates by the ensemble-mean squared distance of their predicted curves to the
     target; return (indices of the best `keep`, their mean scores, a mask of those whose
-    members' predicted peaks spread by more than peak_tolerance of the mean peak)."""
-    scores = np.mean([m.score(candidates, target) for m in members], axis=0)
+    members' predicted peaks spread by more than peak_tolerance of the mean peak).  nets: a
+    Surrogate (all its members) or a list of them."""
+    nets = [nets] if isinstance(nets, Surrogate) else list(nets)
+    scores = np.concatenate([n.score_members(candidates, target) for n in nets]).mean(axis=0)
     best = np.argsort(scores, kind="stable")[:keep]
-    peaks = np.stack([peak_height(m.predict(candidates[best]), days) for m in members])
+    preds = np.concatenate([n.predict_members(candidates[best]) for n in nets])
+    peaks = np.stack([peak_height(p, days) for p in preds])
     mean_peak = np.maximum(np.abs(peaks.mean(axis=0)), 1e-12)
     flagged = (peaks.max(axis=0) - peaks.min(axis=0)) / mean_peak > peak_tolerance
     return best, scores[best], flagged

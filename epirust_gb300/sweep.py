@@ -1,8 +1,9 @@
 """Surrogate training on GPU-ABM ensembles and the surrogate-screened parameter sweep.
 
 train_on_abm():  Latin-hypercube parameter points -> batched GPU-ABM runs -> daily S/E/I/H/R/D
-                 curves (normalised) -> an ensemble of MLPs trained with Adam on the tensor
-                 cores; held-out error against the ABM and against the training-mean curve.
+                 curves (normalised) -> an ensemble of MLPs (one handle, every kernel launch
+                 covering all members) trained with Adam on the tensor cores; held-out error
+                 against the ABM and against the training-mean curve.
 screened_sweep(): a target curve from hidden parameters (ABM at full size), candidates scored
                  by the surrogate ensemble, the best re-run by the batched ABM with several
                  replicates each, and the same ABM budget spent on unscreened candidates.
@@ -45,19 +46,15 @@ def train_on_abm(runs: int = 4096, held_out: int = 512, agents: int = 100_000, d
     t_abm = time.perf_counter() - t0
     n_tr = runs - held_out
     xtr, ytr, xte, yte = u[:n_tr], y[:n_tr], u[n_tr:], y[n_tr:]
-    nets, losses = [], []
     mean, scale = compartment_scaling(ytr, days)
     t0 = time.perf_counter()
-    for m in range(members):
-        net = Surrogate(in_dim=len(PARAMS), out_dim=6 * days, hidden=hidden, hidden_layers=hidden_layers,
-                        batch=batch, seed=seed * 101 + m)
-        net.set_output_scaling(mean, scale)
-        net.set_dataset(xtr, ytr)
-        losses.append(net.train(steps, seed=seed * 7 + m))
-        nets.append(net)
+    net = Surrogate(in_dim=len(PARAMS), out_dim=6 * days, hidden=hidden, hidden_layers=hidden_layers, batch=batch,
+                    seed=seed * 101, members=members)
+    net.set_output_scaling(mean, scale)
+    net.set_dataset(xtr, ytr)
+    losses = np.atleast_2d(net.train(steps, seed=seed * 7))
     t_train = time.perf_counter() - t0
-    preds = np.stack([n.predict(xte) for n in nets])
-    mean_pred = preds.mean(axis=0)
+    mean_pred = net.predict(xte)
     mse_net = float(np.mean((mean_pred - yte) ** 2))
     mse_mean = float(np.mean((ytr.mean(axis=0) - yte) ** 2))
     pe = relative_peak_error(mean_pred, yte, days)
@@ -73,10 +70,10 @@ def train_on_abm(runs: int = 4096, held_out: int = 512, agents: int = 100_000, d
         "held_out_peak_rel_err_median": float(np.median(pe)), "held_out_peak_rel_err_p90": float(np.quantile(pe, 0.9)),
     }
     info["curves"] = y
-    return nets, info
+    return net, info
 
 
-def screened_sweep(nets, candidates: int = 65_536, keep: int = 256, replicates: int = 8, agents: int = 1_000_000,
+def screened_sweep(net, candidates: int = 65_536, keep: int = 256, replicates: int = 8, agents: int = 1_000_000,
                    days: int = 100, seed: int = 99, peak_tolerance: float = 0.05, abm_batch: int = 64,
                    per_agents: int = 100_000):
     grid = grid_for(agents)
@@ -91,9 +88,9 @@ def screened_sweep(nets, candidates: int = 65_536, keep: int = 256, replicates: 
 
     # surrogate screen
     t0 = time.perf_counter()
-    best, best_scores, flagged = screen(nets, cand, target, keep, days, peak_tolerance)
+    best, best_scores, flagged = screen(net, cand, target, keep, days, peak_tolerance)
     t_screen = time.perf_counter() - t0
-    member_preds = np.stack([n.predict(cand[best]) for n in nets])
+    sur_mean = net.predict(cand[best])
 
     def abm(points: np.ndarray, base_seed: int) -> np.ndarray:
         cfgs = [config_for(d, agents, grid, hours, seed=base_seed + 97 * i + r, per_agents=per_agents)
@@ -117,7 +114,6 @@ def screened_sweep(nets, candidates: int = 65_536, keep: int = 256, replicates: 
     pick_r = int(np.argmin(err_r))
 
     # surrogate vs ABM ensemble mean at the screened candidates (the stated error criterion)
-    sur_mean = member_preds.mean(axis=0)
     peak_err = relative_peak_error(sur_mean, mean_s, days)
     per_run_s = t_abm_screened / (keep * replicates)
     abm_only_s = candidates * replicates * per_run_s  # every candidate through the ABM at the measured rate

@@ -46,6 +46,22 @@ def test_struct_layouts_match(engine_built):
     assert L.epi_abi_struct_size(b"epi_geography") == C.sizeof(_lib.EpiGeography)
     assert L.epi_abi_struct_size(b"epi_mlp_config") == C.sizeof(_lib.MlpConfig) == 48
     assert L.epi_abi_struct_size(b"nope") == 0
+    assert (_lib.MlpConfig.members.offset, _lib.MlpConfig.seed.offset) == (36, 40)
+
+
+def test_mlp_config_rejected_before_any_device_call(engine_built):
+    """Invalid network shapes (and more than 64 members) fail with EPI_ERR_CONFIG on the host."""
+    from epirust_gb300 import _lib
+
+    L = _lib.lib()
+    good = dict(in_dim=8, hidden=512, hidden_layers=3, out_dim=600, batch=256, lr=1e-3, beta1=0.9, beta2=0.999,
+                eps=1e-8, members=5, seed=1)
+    for bad in (dict(members=65), dict(hidden=100), dict(batch=200), dict(in_dim=65), dict(hidden_layers=0),
+                dict(lr=0.0)):
+        cfg = _lib.MlpConfig(**{**good, **bad})
+        h = C.c_void_p()
+        assert L.epi_mlp_create(C.byref(cfg), C.byref(h)) == 1, bad  # EPI_ERR_CONFIG
+        assert not h.value
 
 
 def test_config_parse_matches_reference_fixture(engine_built):

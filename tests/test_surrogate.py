@@ -202,13 +202,10 @@ def test_surrogate_gain_over_method_without_it(gpu):
     cfgs = [config_for(d, agents, grid, hours, seed=1000 + i) for i, d in enumerate(denormalise(u))]
     y = simulate_curves(cfgs, days)
     xtr, ytr, xte, yte = u[:640], y[:640], u[640:], y[640:]
-    members = []
-    for m in range(3):
-        net = Surrogate(in_dim=8, out_dim=6 * days, hidden=256, hidden_layers=2, batch=128, seed=10 + m)
-        net.set_dataset(xtr, ytr)
-        net.train(1500, seed=m)
-        members.append(net)
-    pred = np.mean([m.predict(xte) for m in members], axis=0)
+    net = Surrogate(in_dim=8, out_dim=6 * days, hidden=256, hidden_layers=2, batch=128, seed=10, members=3)
+    net.set_dataset(xtr, ytr)
+    net.train(1500, seed=0)
+    pred = net.predict(xte)
     mse_net = np.mean((pred - yte) ** 2)
     mse_mean = np.mean((ytr.mean(axis=0) - yte) ** 2)
     assert mse_net < 0.5 * mse_mean, (mse_net, mse_mean)
@@ -216,7 +213,7 @@ def test_surrogate_gain_over_method_without_it(gpu):
     hidden = np.array([[0.7, 0.6, 0.3, 0.8, 0.4, 0.9, 0.2, 0.7]])
     target = simulate_curves([config_for(denormalise(hidden)[0], agents, grid, hours, seed=99)], days)[0]
     cand = uniform_candidates(4096, 8, seed=8)
-    best, _, _ = screen(members, cand, target, keep=16, days=days)
+    best, _, _ = screen(net, cand, target, keep=16, days=days)
     budget = [config_for(d, agents, grid, hours, seed=2000 + i) for i, d in enumerate(denormalise(cand[best]))]
     rand = cand[np.random.default_rng(9).choice(len(cand), 16, replace=False)]
     budget += [config_for(d, agents, grid, hours, seed=3000 + i) for i, d in enumerate(denormalise(rand))]
@@ -224,5 +221,38 @@ def test_surrogate_gain_over_method_without_it(gpu):
     err = ((abm - target) ** 2).mean(axis=1)
     assert err[:16].min() <= err[16:].min()
     assert np.median(err[:16]) < np.median(err[16:])
-    for m in members:
-        m.close()
+    net.close()
+
+
+@pytest.mark.gpu
+def test_members_equal_lone_networks(gpu):
+    """Member m of a 3-member handle (one launch per kernel for all members) equals a
+    one-member network created with seed + m and trained with shuffle seed + m: parameters
+    and predictions bit for bit (products, bias reductions and Adam are deterministic);
+    scores and losses within float-atomic summation order."""
+    rng = np.random.default_rng(5)
+    shape = dict(out_dim=120, hidden=256, hidden_layers=2, batch=128)
+    x, y = rng.random((640, 8)), rng.random((640, 120)) * 0.5
+    xp = rng.random((300, 8))
+    ens = _net(gpu, seed=20, members=3, **shape)
+    ens.set_dataset(x, y)
+    le = ens.train(40, seed=7)
+    pe, ye, se = ens.get_params(), ens.predict_members(xp), ens.score_members(xp, y[0])
+    assert le.shape == (3, 40) and pe.shape == (3, ens.n_params) and ye.shape == (3, 300, 120)
+    assert np.allclose(ens.predict(xp), ye.mean(axis=0), rtol=1e-6, atol=1e-7)
+    g_loss, g = ens.gradients(x[:128], y[:128])
+    for m in range(3):
+        one = _net(gpu, seed=20 + m, **shape)
+        one.set_dataset(x, y)
+        lo = one.train(40, seed=7 + m)
+        assert np.array_equal(one.get_params(), pe[m]), m
+        assert np.array_equal(one.predict(xp), ye[m]), m
+        assert np.allclose(one.score(xp, y[0]), se[m], rtol=1e-5, atol=1e-7), m
+        assert np.allclose(lo, le[m], rtol=1e-4), m
+        l1, g1 = one.gradients(x[:128], y[:128])
+        assert np.array_equal(g1, g[m]) and l1 == pytest.approx(float(g_loss[m]), rel=1e-5), m
+        one.close()
+    # set_params on the stack == per-member set_params
+    ens.set_params(pe[::-1].copy())
+    assert np.array_equal(ens.get_params(), pe[::-1])
+    ens.close()
