@@ -61,7 +61,7 @@ struct epi_engine {
     size_t plane_bytes = 0;    // all bordered byte planes
     size_t claim_cells = 0;    // all claim planes
     int grid_blocks = 0;       // grid of the counting kernels (k_decide, k_sleep)
-    int commit_slots = kCommitSlots;  // slots per k_commit thread (1, 2 or 4)
+    int commit_slots = kCommitSlots;  // slots per k_commit thread and round (1 .. 8)
     int commit_blocks = 0;
     int resident_blocks = 0;   // SMs x resident k_decide blocks per SM
     // device
@@ -74,17 +74,20 @@ struct epi_engine {
     uint8_t* d_danger = nullptr;  // infectious-neighbour counts, same layout as d_plane
     uint32_t* d_claim = nullptr;
     uint32_t* d_counts = nullptr;  // [hour of segment][replicate][8]
-    uint32_t* d_hour_base = nullptr;
+    SegDev* d_seg = nullptr;       // hour base of the running piece and first hour of the chain
+    uint32_t* d_ivn = nullptr;     // per replicate: the guard's new-infections figure
     int* d_err = nullptr;
     unsigned long long* d_scratch = nullptr;
     uint32_t counts_capacity = 0;  // hours
     // host
     uint32_t* h_counts = nullptr;  // pinned mirror of d_counts
-    uint32_t* h_hour_base = nullptr;
+    SegDev* h_seg = nullptr;       // pinned staging of d_seg and d_ivn
+    uint32_t* h_ivn = nullptr;
+    int halt_row = -1;             // chain offset of the row the guard marked in the last chain
     cudaStream_t stream = nullptr;
     bool own_stream = false;
-    // hour graphs by (first hour mod 24 + 24 * window offset, hours, profiling); a profiling
-    // graph carries an event-record node before and after each kernel
+    // piece graphs by (first hour mod 24, hours, profiling | stream << 1 | run loop << 2); a
+    // profiling graph carries an event-record node before and after each kernel
     struct HourGraph {
         cudaGraphExec_t exec = nullptr;
         std::vector<TimedLaunch> events;
@@ -136,6 +139,29 @@ static thread_local std::string g_create_error;
     } while (0)
 
 static Rect to_rect(const epi_area& a) { return Rect{a.x0, a.y0, a.x1, a.y1}; }
+
+#ifndef EPI_DEPENDENT_LAUNCH
+#define EPI_DEPENDENT_LAUNCH 1
+#endif
+
+// Launch of an hour kernel with programmatic stream serialisation: its blocks may be
+// scheduled before the previous kernel of the stream has finished and wait on the device
+// (dep_wait) for it, which hides the launch gap between the hour's kernels.  Captured into
+// the hour graphs as programmatic edges.
+template <typename... KArgs, typename... Args>
+static cudaError_t launch_hour_kernel(void (*kern)(KArgs...), uint32_t blocks, cudaStream_t s, Args&&... args) {
+    cudaLaunchConfig_t cfg = {};
+    cfg.gridDim = dim3(blocks);
+    cfg.blockDim = dim3(kThreads);
+    cfg.dynamicSmemBytes = 0;
+    cfg.stream = s;
+    cudaLaunchAttribute at[1];
+    at[0].id = cudaLaunchAttributeProgrammaticStreamSerialization;
+    at[0].val.programmaticStreamSerializationAllowed = EPI_DEPENDENT_LAUNCH;
+    cfg.attrs = at;
+    cfg.numAttrs = 1;
+    return cudaLaunchKernelEx(&cfg, kern, std::forward<Args>(args)...);
+}
 
 // Device parameters of one world: areas, random key, disease thresholds.
 static DevParams make_dev_params(const epi_params& p, const epi_geography& geo0, uint32_t n) {
@@ -254,7 +280,15 @@ static void destroy_graphs(epi_engine* h) {
 
 static int push_params(epi_engine* h) {
     std::vector<DevParams> all(h->R());
-    for (uint32_t r = 0; r < h->R(); ++r) all[r] = h->reps[r].hp;
+    for (uint32_t r = 0; r < h->R(); ++r) {
+        Replica& rep = h->reps[r];
+        const GuardParams g = guard_params(rep.p, rep.iv, rep.geo.hospital);
+        rep.hp.guard_flags = g.flags;
+        rep.hp.lock_threshold = g.lock_threshold;
+        rep.hp.spread_threshold = g.spread_threshold;
+        rep.hp.occ_threshold = g.occ_threshold;
+        all[r] = rep.hp;
+    }
     CK(cudaMemcpyAsync(h->d_params, all.data(), all.size() * sizeof(DevParams), cudaMemcpyHostToDevice, h->stream));
     CK(cudaStreamSynchronize(h->stream));
     return EPI_OK;
@@ -278,12 +312,12 @@ static int ensure_counts(epi_engine* h, uint32_t hours_needed) {
 // ------------------------------------------------------------------ the hour loop
 using DecideKernel = void (*)(const DevParams*, const uint32_t*, uint32_t, const uint32_t*, uint2*, const uint32_t*,
                               const uint32_t*, uint32_t*, const uint8_t*, const uint8_t*, uint32_t*, uint32_t*, uint32_t*,
-                              uint32_t*, const uint32_t*, uint32_t, int*, const uint32_t*);
+                              HourArgs, int*);
 
 // Hours 2..6 of a day change nothing once hour 1 has sent everyone but hospital staff home
 // (routine, citizen/mod.rs:243-247, sets current_area = home_location and nothing else), so
-// when the previous hour ran in the same segment the hour's kernel is skipped and its
-// counts row repeats the previous one.
+// when the previous hour ran in the same chain the hour's kernel is skipped and its counts
+// row repeats the previous one.  (A piece that starts at hours 2..6 always starts a chain.)
 static bool sleep_hour_skipped(uint32_t first_hour, uint32_t k) {
     const uint32_t hod = (first_hour + k) % 24u;
     return k > 0 && hod >= 2u && hod <= 6u;
@@ -307,60 +341,75 @@ static int commit_blocks_for(uint32_t slots, int per_thread = kCommitSlots) {
     return (int)std::max<uint32_t>(1u, (slots + per_block - 1) / per_block);
 }
 
-// k_commit with S slots per thread.
+// k_commit with S slots per thread and round.
 using CommitKernel = void (*)(const DevParams*, const uint32_t*, uint32_t, uint32_t*, const uint32_t*, uint8_t*,
-                              uint8_t*, const uint32_t*, const uint32_t*, const uint32_t*, uint32_t, const uint32_t*);
+                              uint8_t*, uint32_t*, const uint32_t*, HourArgs, uint64_t);
 static CommitKernel commit_kernel(int slots_per_thread) {
     switch (slots_per_thread) {
         case 1: return k_commit<1>;
         case 2: return k_commit<2>;
-        default: return k_commit<4>;
+        case 3: return k_commit<3>;
+        case 4: return k_commit<4>;
+        case 5: return k_commit<5>;
+        case 6: return k_commit<6>;
+        case 7: return k_commit<7>;
+        default: return k_commit<8>;
     }
 }
-// Kernels of hours hour_base .. hour_base + nh - 1 (hour_base read on the device).
-// Offset within the segment of the first hour that opens a new claim window, or nh; later
-// windows open every kClaimWindow hours after it.
-static uint32_t window_start_offset(uint32_t first_hour, uint32_t nh) {
-    const uint32_t k = (kClaimWindow - first_hour % kClaimWindow) % kClaimWindow;
-    return (k > 0 && k < nh) ? k : nh;
+
+// k_commit grid for S slots per thread: every slot once.  (Capping it at one wave of
+// resident blocks that loop over the rest was measured slower: the block scheduler's later
+// waves keep more loads in flight than a second round of the same threads.)
+static int commit_grid(epi_engine* h, int S, int* out) {
+    *out = commit_blocks_for(h->slots, S);
+    return EPI_OK;
 }
 
-static int enqueue_hours(epi_engine* h, uint32_t first_hour, uint32_t nh) {
-    const size_t row_words = (size_t)h->R() * 8;
-    CK(cudaMemsetAsync(h->d_counts, 0, (size_t)nh * row_words * sizeof(uint32_t), h->stream));
-    if (h->stream_file) CK(cudaMemsetAsync(h->d_exc_n, 0, (size_t)nh * sizeof(uint32_t), h->stream));
+// Kernels of one piece: hours first_hour .. first_hour + nh - 1 of a chain; the hour base is
+// read on the device, so a captured piece serves every start hour with the same hour of the
+// day.  A piece that does not end its chain ends after an hour of day 0.  In the run loop a
+// guard follows every hour of day 0.
+static int enqueue_piece(epi_engine* h, uint32_t first_hour, uint32_t nh) {
+    const uint32_t row_words = h->R() * 8u;
     const uint32_t n_chunks = h->slots / kChunk;
-    int last_row = -1;  // the latest hour of the segment whose counts the kernels computed
+    int last_row = -1;  // the latest hour of the piece whose counts the kernels computed
     for (uint32_t k = 0; k < nh; ++k) {
         const uint32_t hod = (first_hour + k) % 24u;
-        uint32_t* rows = h->d_counts + (size_t)k * row_words;
-        const uint32_t* prev = h->stop_rule && last_row >= 0 ? h->d_counts + (size_t)last_row * row_words : nullptr;
-        if (k > 0 && (first_hour + k) % kClaimWindow == 0) CK(cudaMemsetAsync(h->d_claim, 0xFF, h->claim_cells * sizeof(uint32_t), h->stream));
-        if (h->stream_file) {  // record the previous hour's end state before this hour changes it
-            if (k > 0) {
-                const uint32_t n = h->reps[0].n;
-                k_state_delta<<<(n + kThreads - 1) / kThreads, kThreads, 0, h->stream>>>(
-                    n, h->d_pos, h->d_st, h->d_prev, h->d_codes + (size_t)(k - 1) * h->slots,
-                    h->d_exc + (size_t)(k - 1) * h->slots, h->d_exc_n + (k - 1));
-                CK(cudaGetLastError());
-            }
+        // rows back to the previous computed hour: within the piece, or the hour before it
+        // (a day boundary, computed) unless the piece starts the chain (checked on the device)
+        const uint32_t prev_back = !h->stop_rule ? 0u : (last_row >= 0 ? k - (uint32_t)last_row : 1u);
+        const HourArgs ha{h->d_seg, h->d_counts, row_words, k, prev_back};
+        if (h->stream_file && k > 0) {  // record the previous hour's end state before this hour changes it
+            const uint32_t n = h->reps[0].n;
+            k_state_delta<<<(n + kThreads - 1) / kThreads, kThreads, 0, h->stream>>>(
+                n, h->d_pos, h->d_st, h->d_prev, h->d_codes + (size_t)(k - 1) * h->slots,
+                h->d_exc + (size_t)(k - 1) * h->slots, h->d_exc_n + (k - 1));
+            CK(cudaGetLastError());
         }
         if (sleep_hour_skipped(first_hour, k)) continue;
         last_row = (int)k;
         if (hod >= 1u && hod <= 6u) {
-            LAUNCH(kKSleep, (k_sleep<<<h->grid_blocks, kThreads, 0, h->stream>>>(h->d_params, h->d_chunk_rep, n_chunks,
-                                                                                  h->d_st, rows, prev)));
+            LAUNCH(kKSleep, CK(launch_hour_kernel(k_sleep, h->grid_blocks, h->stream, (const DevParams*)h->d_params,
+                                                  (const uint32_t*)h->d_chunk_rep, n_chunks, h->d_st, ha)));
         } else {
             const DecideKernel decide = decide_kernel(hod);
-            LAUNCH(kKDecide, (decide<<<h->grid_blocks, kThreads, 0, h->stream>>>(
-                                  h->d_params, h->d_chunk_rep, n_chunks, h->d_pos, h->d_st, h->d_home, h->d_work, h->d_wsa,
-                                  h->d_plane, h->d_danger, h->d_claim, h->d_tgt, h->d_lost, rows, h->d_hour_base, k,
-                                  h->d_err, prev)));
+            LAUNCH(kKDecide, CK(launch_hour_kernel(
+                                  decide, h->grid_blocks, h->stream, (const DevParams*)h->d_params,
+                                  (const uint32_t*)h->d_chunk_rep, n_chunks, (const uint32_t*)h->d_pos, h->d_st,
+                                  (const uint32_t*)h->d_home, (const uint32_t*)h->d_work, h->d_wsa,
+                                  (const uint8_t*)h->d_plane, (const uint8_t*)h->d_danger, h->d_claim, h->d_tgt, h->d_lost,
+                                  ha, h->d_err)));
             const CommitKernel commit = commit_kernel(h->commit_slots);
-            LAUNCH(kKCommit, (commit<<<h->commit_blocks, kThreads, 0, h->stream>>>(h->d_params, h->d_chunk_rep, h->slots,
-                                                                                   h->d_pos, h->d_tgt, h->d_plane, h->d_danger,
-                                                                                   h->d_claim, h->d_lost, h->d_hour_base,
-                                                                                   k, prev)));
+            LAUNCH(kKCommit, CK(launch_hour_kernel(commit, h->commit_blocks, h->stream, (const DevParams*)h->d_params,
+                                                   (const uint32_t*)h->d_chunk_rep, h->slots, h->d_pos,
+                                                   (const uint32_t*)h->d_tgt, h->d_plane, h->d_danger, h->d_claim,
+                                                   (const uint32_t*)h->d_lost, ha, (uint64_t)h->claim_cells)));
+        }
+        // the run loop's guard after every day boundary but the piece's last hour (the piece
+        // end below takes that one)
+        if (h->stop_rule && hod == 0u && k + 1 < nh) {
+            k_piece_end<<<1, kThreads, 0, h->stream>>>(h->d_params, h->R(), h->d_seg, h->d_counts, row_words, k, 0u, h->d_ivn);
+            CK(cudaGetLastError());
         }
     }
     if (h->stream_file) {
@@ -370,25 +419,71 @@ static int enqueue_hours(epi_engine* h, uint32_t first_hour, uint32_t nh) {
             h->d_exc_n + (nh - 1));
         CK(cudaGetLastError());
     }
-    CK(cudaMemcpyAsync(h->h_counts, h->d_counts, (size_t)nh * row_words * sizeof(uint32_t), cudaMemcpyDeviceToHost,
-                       h->stream));
+    const bool guard_last = h->stop_rule && (first_hour + nh - 1) % 24u == 0u;
+    k_piece_end<<<1, kThreads, 0, h->stream>>>(h->d_params, h->R(), h->d_seg, h->d_counts, row_words,
+                                               guard_last ? nh - 1 : kNoGuard, nh, h->d_ivn);
+    CK(cudaGetLastError());
     return EPI_OK;
 }
 
-static int check_error_flag(epi_engine* h) {
-    int e = 0;
-    CK(cudaMemcpyAsync(&e, h->d_err, sizeof(int), cudaMemcpyDeviceToHost, h->stream));
-    CK(cudaStreamSynchronize(h->stream));
-    if (e) {
-        h->err = "device invariant violated (flag " + std::to_string(e) + "): a rule addressed a cell outside the plane";
-        return EPI_ERR_INVARIANT;
+// Kernel launches of a piece, for the launch counter.
+static uint64_t piece_launches(const epi_engine* h, uint32_t first_hour, uint32_t nh) {
+    uint64_t n = 1;  // k_piece_end
+    for (uint32_t k = 0; k < nh; ++k) {
+        const uint32_t hod = (first_hour + k) % 24u;
+        if (h->stream_file) n += 1;  // k_state_delta
+        if (h->stop_rule && hod == 0u && k + 1 < nh) n += 1;
+        if (sleep_hour_skipped(first_hour, k)) continue;
+        n += (hod >= 1u && hod <= 6u) ? 1u : 2u;
     }
+    return n;
+}
+
+// The graph of a piece (captured on first use).
+static int piece_graph(epi_engine* h, uint32_t first_hour, uint32_t nh, cudaGraphExec_t* out,
+                       std::vector<TimedLaunch>** events) {
+    auto key = std::make_tuple(first_hour % 24u, nh,
+                               (h->profiling ? 1u : 0u) | (h->stream_file ? 2u : 0u) | (h->stop_rule ? 4u : 0u));
+    auto it = h->graphs.find(key);
+    if (it == h->graphs.end()) {
+        epi_engine::HourGraph hg;
+        cudaGraph_t g;
+        CK(cudaStreamBeginCapture(h->stream, cudaStreamCaptureModeThreadLocal));
+        h->capture = &hg.events;
+        int rc = enqueue_piece(h, first_hour, nh);
+        h->capture = nullptr;
+        cudaError_t ce = cudaStreamEndCapture(h->stream, &g);
+        if (rc == EPI_OK && ce == cudaSuccess) {
+            ce = cudaGraphInstantiate(&hg.exec, g, 0);
+            cudaGraphDestroy(g);
+        }
+        if (rc != EPI_OK || ce != cudaSuccess) {
+            for (auto& t : hg.events) { cudaEventDestroy(t.begin); cudaEventDestroy(t.end); }
+            if (rc) return rc;
+            h->err = std::string("hour graph: ") + cudaGetErrorString(ce);
+            return EPI_ERR_CUDA;
+        }
+        it = h->graphs.emplace(key, std::move(hg)).first;
+    }
+    *out = it->second.exec;
+    *events = &it->second.events;
     return EPI_OK;
 }
 
-// Simulate hours first_hour .. first_hour + nh - 1 for every active replicate; the counts
-// of hour k of replicate r land in h_counts[(k * R + r) * 8 ..].
+static int check_error_flag(epi_engine* h);
+
+// Longest piece (one captured graph): eight days.  Consecutive graph launches leave a gap of
+// several microseconds on the device, so pieces are long; their capture is paid once per
+// engine and shape.
+constexpr uint32_t kPieceHours = 24u * 8u;
+
+// Simulate hours first_hour .. first_hour + nh - 1 for every active replicate as one chain:
+// pieces of whole days, launched back to back with one host synchronisation at the end
+// (after each piece when profiling, whose events are read per launch).  The
+// counts of hour k of replicate r land in h_counts[(k * R + r) * 8 ..]; in the run loop,
+// h->halt_row is the chain offset of a row the guard marked, or -1.
 static int run_hours_chunk(epi_engine* h, uint32_t first_hour, uint32_t nh) {
+    h->halt_row = -1;
     if (nh == 0) return EPI_OK;
     if ((uint64_t)first_hour + nh > 0xFFFFFFFFull) { h->err = "hour out of range"; return EPI_ERR_ARG; }
     int rc = ensure_counts(h, nh);
@@ -400,52 +495,46 @@ static int run_hours_chunk(epi_engine* h, uint32_t first_hour, uint32_t nh) {
     if (h->last_claim_hour >= (int64_t)first_hour)  // loss marks of hours about to run again
         CK(cudaMemsetAsync(h->d_lost, 0xFF, (size_t)h->slots * sizeof(uint32_t), h->stream));
     h->last_claim_hour = (int64_t)first_hour + nh - 1;
-    *h->h_hour_base = first_hour;
-    CK(cudaMemcpyAsync(h->d_hour_base, h->h_hour_base, sizeof(uint32_t), cudaMemcpyHostToDevice, h->stream));
-    {
-        // the kernel sequence depends on the hours of the day and on where a claim window opens
-        auto key = std::make_tuple(first_hour % 24u + 24u * window_start_offset(first_hour, nh), nh,
-                                   (h->profiling ? 1u : 0u) | (h->stream_file ? 2u : 0u) | (h->stop_rule ? 4u : 0u));
-        auto it = h->graphs.find(key);
-        if (it == h->graphs.end()) {
-            epi_engine::HourGraph hg;
-            cudaGraph_t g;
-            CK(cudaStreamBeginCapture(h->stream, cudaStreamCaptureModeThreadLocal));
-            h->capture = &hg.events;
-            rc = enqueue_hours(h, first_hour, nh);
-            h->capture = nullptr;
-            cudaError_t ce = cudaStreamEndCapture(h->stream, &g);
-            if (rc == EPI_OK && ce == cudaSuccess) {
-                ce = cudaGraphInstantiate(&hg.exec, g, 0);
-                cudaGraphDestroy(g);
-            }
-            if (rc != EPI_OK || ce != cudaSuccess) {
-                for (auto& t : hg.events) { cudaEventDestroy(t.begin); cudaEventDestroy(t.end); }
-                if (rc) return rc;
-                h->err = std::string("hour graph: ") + cudaGetErrorString(ce);
-                return EPI_ERR_CUDA;
-            }
-            it = h->graphs.emplace(key, std::move(hg)).first;
+    const size_t row_words = (size_t)h->R() * 8;
+    CK(cudaMemsetAsync(h->d_counts, 0, (size_t)nh * row_words * sizeof(uint32_t), h->stream));
+    if (h->stream_file) CK(cudaMemsetAsync(h->d_exc_n, 0, (size_t)nh * sizeof(uint32_t), h->stream));
+    h->h_seg->hour_base = first_hour;
+    h->h_seg->first = first_hour;
+    CK(cudaMemcpyAsync(h->d_seg, h->h_seg, sizeof(SegDev), cudaMemcpyHostToDevice, h->stream));
+    // pieces: at most kPieceHours, ending after an hour of day 0 unless they end the chain, so
+    // that a chain of whole days replays one graph; the stream's chunks stay whole (their
+    // code buffers are indexed by the hour)
+    for (uint32_t k0 = 0; k0 < nh;) {
+        uint32_t len = nh - k0;
+        if (!h->stream_file && len > kPieceHours) {
+            const uint32_t head = (24u - (first_hour + k0) % 24u) % 24u + 1u;  // through the next hour of day 0
+            len = head + (kPieceHours - std::min(head, kPieceHours)) / 24u * 24u;
         }
-        CK(cudaGraphLaunch(it->second.exec, h->stream));
-        h->pending.insert(h->pending.end(), it->second.events.begin(), it->second.events.end());
+        cudaGraphExec_t exec;
+        std::vector<TimedLaunch>* events;
+        rc = piece_graph(h, first_hour + k0, len, &exec, &events);
+        if (rc) return rc;
+        CK(cudaGraphLaunch(exec, h->stream));
+        h->kernels_launched += piece_launches(h, first_hour + k0, len);
+        if (h->profiling) {  // the piece's event nodes hold this launch's times until its next launch
+            h->pending.insert(h->pending.end(), events->begin(), events->end());
+            CK(cudaStreamSynchronize(h->stream));
+            rc = harvest_events(h);
+            if (rc) return rc;
+        }
+        k0 += len;
     }
+    CK(cudaMemcpyAsync(h->h_counts, h->d_counts, (size_t)nh * row_words * sizeof(uint32_t), cudaMemcpyDeviceToHost,
+                       h->stream));
     CK(cudaStreamSynchronize(h->stream));
-    for (uint32_t k = 0; k < nh; ++k) {
-        const uint32_t hod = (first_hour + k) % 24u;
-        if (sleep_hour_skipped(first_hour, k)) {
-            std::memcpy(h->h_counts + (size_t)k * h->R() * 8, h->h_counts + (size_t)(k - 1) * h->R() * 8,
-                        (size_t)h->R() * 8 * sizeof(uint32_t));
-            continue;
-        }
-        h->kernels_launched += (hod >= 1u && hod <= 6u) ? 1u : 2u;
-    }
-    rc = harvest_events(h);
-    if (rc) return rc;
+    for (uint32_t k = 1; k < nh; ++k)
+        if (sleep_hour_skipped(first_hour, k))
+            std::memcpy(h->h_counts + (size_t)k * row_words, h->h_counts + (size_t)(k - 1) * row_words,
+                        row_words * sizeof(uint32_t));
     rc = check_error_flag(h);
     if (rc) return rc;
-    std::vector<uint8_t> ended(h->R(), 0);  // stop rule met at an earlier hour of this segment
-    for (uint32_t k = 0; k < nh; ++k) {
+    std::vector<uint8_t> ended(h->R(), 0);  // stop rule met at an earlier hour of this chain
+    for (uint32_t k = 0; k < nh && h->halt_row < 0; ++k) {
         for (uint32_t r = 0; r < h->R(); ++r) {
             if (!h->reps[r].active || ended[r]) continue;
             const uint32_t* c = h->h_counts + ((size_t)k * h->R() + r) * 8;
@@ -457,6 +546,18 @@ static int run_hours_chunk(epi_engine* h, uint32_t first_hour, uint32_t nh) {
                 return EPI_ERR_INVARIANT;
             }
         }
+        if (h->stop_rule && h->h_counts[(size_t)k * row_words + 6] != 0u) h->halt_row = (int)k;  // later rows did not run
+    }
+    return EPI_OK;
+}
+
+static int check_error_flag(epi_engine* h) {
+    int e = 0;
+    CK(cudaMemcpyAsync(&e, h->d_err, sizeof(int), cudaMemcpyDeviceToHost, h->stream));
+    CK(cudaStreamSynchronize(h->stream));
+    if (e) {
+        h->err = "device invariant violated (flag " + std::to_string(e) + "): a rule addressed a cell outside the plane";
+        return EPI_ERR_INVARIANT;
     }
     return EPI_OK;
 }
@@ -492,29 +593,44 @@ static int stream_write(epi_engine* h, uint32_t first_hour, uint32_t m) {
 // Hours first_hour .. first_hour + nh - 1 (see run_hours_chunk); with the stream open they run
 // in chunks of at most kStreamChunk hours, each written out before the next.
 static int run_hours(epi_engine* h, uint32_t first_hour, uint32_t nh) {
+    if (h->stop_rule) {  // the guard's new-infections figures as the host has them (the chunks carry them on)
+        CK(cudaStreamSynchronize(h->stream));  // the pinned staging may still feed an earlier copy
+        for (uint32_t r = 0; r < h->R(); ++r) h->h_ivn[r] = h->reps[r].iv.new_infections_in_a_day;
+        CK(cudaMemcpyAsync(h->d_ivn, h->h_ivn, h->R() * sizeof(uint32_t), cudaMemcpyHostToDevice, h->stream));
+    }
     if (!h->stream_file) return run_hours_chunk(h, first_hour, nh);
     int rc = ensure_counts(h, std::max(nh, kStreamChunk));
     if (rc) return rc;
     const size_t row = (size_t)h->R() * 8;
     std::vector<uint32_t> all((size_t)nh * row, 0u);
+    int halt = -1;
     for (uint32_t k0 = 0; k0 < nh; k0 += kStreamChunk) {
         const uint32_t m = std::min(kStreamChunk, nh - k0);
         rc = run_hours_chunk(h, first_hour + k0, m);
         if (rc) return rc;
         // in the run loop the record ends with the hour the stop rule fires (the reference
-        // publishes no later hour)
+        // publishes no later hour), or with a row the guard marked (the hours after it did
+        // not run; the run loop runs them again)
+        // (each chunk is a chain of its own, so the host, not the device, ends the run here)
         uint32_t keep = m;
+        bool over = false;
         if (h->stop_rule)
             for (uint32_t k = 0; k < m; ++k) {
                 const uint32_t* c = h->h_counts + (size_t)k * row;
-                if ((c[1] | c[2] | c[3]) == 0u) { keep = k + 1; break; }
+                if ((c[1] | c[2] | c[3]) == 0u) { keep = k + 1; over = true; break; }
             }
+        if (h->halt_row >= 0 && (uint32_t)h->halt_row < keep) {
+            keep = (uint32_t)h->halt_row + 1;
+            halt = (int)(k0 + (uint32_t)h->halt_row);
+            over = true;
+        }
         rc = stream_write(h, first_hour + k0, keep);
         if (rc) return rc;
         std::memcpy(all.data() + (size_t)k0 * row, h->h_counts, (size_t)keep * row * sizeof(uint32_t));
-        if (keep < m) break;
+        if (over) break;
     }
     std::memcpy(h->h_counts, all.data(), all.size() * sizeof(uint32_t));
+    h->halt_row = halt;
     return EPI_OK;
 }
 
@@ -573,7 +689,8 @@ static void grow_hospital(epi_engine* h, uint32_t r) {
 }
 
 // process_interventions of one replicate; returns EPI_IV_* bits in *applied.  Parameter
-// changes (hospital) are left for the caller to push.
+// changes (the hospital, and the device guard's armed triggers after any action) are left
+// for the caller to push.
 static int process_interventions(epi_engine* h, uint32_t r, const epi_counts& c, uint32_t* applied, bool* params_dirty) {
     Replica& rep = h->reps[r];
     InterventionActions a = decide_interventions(rep.p, rep.iv, c, rep.geo.hospital);
@@ -581,10 +698,8 @@ static int process_interventions(epi_engine* h, uint32_t r, const epi_counts& c,
     if (a.vaccinate && (rc = vaccinate(h, r, c.hour, a.vaccinate_percent))) return rc;
     if (a.lock && (rc = lock_city(h, r, 1))) return rc;
     if (a.unlock && (rc = lock_city(h, r, 0))) return rc;
-    if (a.grow_hospital) {
-        grow_hospital(h, r);
-        *params_dirty = true;
-    }
+    if (a.grow_hospital) grow_hospital(h, r);
+    if (a.applied) *params_dirty = true;
     if (applied) *applied = a.applied;
     return EPI_OK;
 }
@@ -612,6 +727,11 @@ static int run_loop(epi_engine* h) {
     return rc ? rc : rc2;
 }
 
+// Longest chain of the run loop: a chain that the guard halts early has launched its later
+// pieces for nothing (their kernels see the mark and return at once), so the cap bounds that
+// waste while the host synchronises once per chain instead of once per day.
+constexpr uint32_t kChainHours = 24u * 8u;
+
 static int run_loop_body(epi_engine* h) {
     uint32_t last = 0;  // last simulated hour over all replicates
     for (auto& rep : h->reps) {
@@ -631,38 +751,53 @@ static int run_loop_body(epi_engine* h) {
             if (rc) return rc;
             dirty = false;
         }
-        uint32_t end = hour;
-        for (;; ++end) {
-            if (end >= last) break;
-            bool boundary = false;
-            for (const auto& rep : h->reps)
-                if (rep.active && (is_event_hour(rep.p, end) || end + 1 == rep.p.hours)) boundary = true;
-            if (boundary) break;
+        // the chain ends at the first hour where the host must act whatever the counts are: a
+        // replicate's final hour or fixed intervention; data-dependent triggers halt it on
+        // the device at the day boundary where they fire
+        uint64_t end = std::min<uint64_t>(last, (uint64_t)hour + kChainHours - 1);
+        for (const auto& rep : h->reps) {
+            if (!rep.active) continue;
+            end = std::min<uint64_t>(end, rep.p.hours - 1);
+            end = std::min<uint64_t>(end, next_fixed_event(rep.p, rep.iv, hour));
         }
-        const uint32_t nh = end - hour + 1;
+        const uint32_t nh = (uint32_t)end - hour + 1;
         int rc = run_hours(h, hour, nh);
         if (rc) return rc;
-        for (uint32_t r = 0; r < h->R(); ++r) {
-            Replica& rep = h->reps[r];
-            if (!rep.active) continue;
-            for (uint32_t k = 0; k < nh; ++k) {
-                const uint32_t hr = hour + k;
+        uint32_t next = (uint32_t)end + 1;
+        for (uint32_t k = 0; k < nh; ++k) {
+            const uint32_t hr = hour + k;
+            bool acted = false;
+            for (uint32_t r = 0; r < h->R(); ++r) {
+                Replica& rep = h->reps[r];
+                if (!rep.active) continue;
                 const epi_counts c = counts_of(h, k, r, hr);
                 rep.rows.push_back(c);
-                if (k + 1 == nh) {  // interventions only fire at intervention points, which end segments
-                    rc = process_interventions(h, r, c, nullptr, &dirty);
+                if (is_event_hour(rep.p, hr)) {
+                    uint32_t applied = 0;
+                    rc = process_interventions(h, r, c, &applied, &dirty);
                     if (rc) return rc;
+                    acted |= applied != 0u;
                 }
                 const bool stop = c.exposed == 0 && c.infected == 0 && c.hospitalized == 0;
                 if (stop || hr + 1 >= rep.p.hours) {
                     rep.active = false;
                     rep.hp.active = 0;
                     dirty = true;
-                    break;
                 }
             }
+            const bool halted = h->halt_row == (int)k;
+            if (acted && !halted && k + 1 < nh) {
+                // an intervention the device guard did not see: the later hours ran without it
+                h->err = "run loop: an intervention fired at hour " + std::to_string(hr) +
+                         " inside a chain without the device guard's mark";
+                return EPI_ERR_INVARIANT;
+            }
+            if (acted || halted) {
+                next = hr + 1;
+                break;
+            }
         }
-        hour = end + 1;
+        hour = next;
     }
     if (dirty) return push_params(h);
     return EPI_OK;
@@ -674,10 +809,11 @@ static void free_device(epi_engine* h) {
     stream_free(h);
     cudaFree(h->d_params); cudaFree(h->d_chunk_rep); cudaFree(h->d_pos); cudaFree(h->d_home); cudaFree(h->d_work);
     cudaFree(h->d_wsa); cudaFree(h->d_tgt); cudaFree(h->d_lost); cudaFree(h->d_st); cudaFree(h->d_plane); cudaFree(h->d_danger); cudaFree(h->d_claim);
-    cudaFree(h->d_counts); cudaFree(h->d_hour_base); cudaFree(h->d_err); cudaFree(h->d_scratch);
+    cudaFree(h->d_counts); cudaFree(h->d_seg); cudaFree(h->d_ivn); cudaFree(h->d_err); cudaFree(h->d_scratch);
     cudaFree(h->s_pos); cudaFree(h->s_wsa); cudaFree(h->s_st); cudaFree(h->s_plane); cudaFree(h->s_danger);
     if (h->h_counts) cudaFreeHost(h->h_counts);
-    if (h->h_hour_base) cudaFreeHost(h->h_hour_base);
+    if (h->h_seg) cudaFreeHost(h->h_seg);
+    if (h->h_ivn) cudaFreeHost(h->h_ivn);
     for (auto& pe : h->pending)
         if (pe.pooled) { cudaEventDestroy(pe.begin); cudaEventDestroy(pe.end); }
     for (auto e : h->event_pool) cudaEventDestroy(e);
@@ -853,7 +989,10 @@ static int engine_init(epi_engine* h, const epi_params* params, const epi_agent_
     const uint64_t n_chunks = slots / kChunk;
     h->resident_blocks = sms * per_sm;
     h->grid_blocks = (int)std::min<uint64_t>(n_chunks, (uint64_t)h->resident_blocks);
-    h->commit_blocks = commit_blocks_for(h->slots, h->commit_slots);
+    {
+        const int rc = commit_grid(h, h->commit_slots, &h->commit_blocks);
+        if (rc) return rc;
+    }
     CK(cudaStreamCreateWithFlags(&h->stream, cudaStreamNonBlocking));
     h->own_stream = true;
     CK(cudaMalloc(&h->d_params, R * sizeof(DevParams)));
@@ -877,10 +1016,13 @@ static int engine_init(epi_engine* h, const epi_params* params, const epi_agent_
     CK(cudaMalloc(&h->d_plane, h->plane_bytes));
     CK(cudaMalloc(&h->d_danger, h->plane_bytes));
     CK(cudaMalloc(&h->d_claim, h->claim_cells * sizeof(uint32_t)));
-    CK(cudaMalloc(&h->d_hour_base, sizeof(uint32_t)));
+    CK(cudaMalloc(&h->d_seg, sizeof(SegDev)));
+    CK(cudaMalloc(&h->d_ivn, R * sizeof(uint32_t)));
+    CK(cudaMemset(h->d_ivn, 0, R * sizeof(uint32_t)));
     CK(cudaMalloc(&h->d_err, sizeof(int)));
     CK(cudaMalloc(&h->d_scratch, 4 * sizeof(unsigned long long)));
-    CK(cudaMallocHost(&h->h_hour_base, sizeof(uint32_t)));
+    CK(cudaMallocHost(&h->h_seg, sizeof(SegDev)));
+    CK(cudaMallocHost(&h->h_ivn, R * sizeof(uint32_t)));
     int rc = ensure_counts(h, 48);
     if (rc) return rc;
     if (!recs) {
@@ -1001,14 +1143,18 @@ static int restore_state(epi_engine* h);
 
 static int set_launch_shape(epi_engine* h, uint32_t decide_blocks, uint32_t commit_slots) {
     const uint32_t n_chunks = h->slots / kChunk;
-    if (decide_blocks == 0 || decide_blocks > n_chunks || !(commit_slots == 1 || commit_slots == 2 || commit_slots == 4)) {
-        h->err = "launch shape: k_decide blocks in [1, " + std::to_string(n_chunks) + "], k_commit slots 1, 2 or 4";
+    if (decide_blocks == 0 || decide_blocks > n_chunks || commit_slots == 0 || commit_slots > (uint32_t)kMaxCommitSlots) {
+        h->err = "launch shape: k_decide blocks in [1, " + std::to_string(n_chunks) + "], k_commit slots in [1, " +
+                 std::to_string(kMaxCommitSlots) + "]";
         return EPI_ERR_ARG;
     }
     CK(cudaStreamSynchronize(h->stream));
     h->grid_blocks = (int)decide_blocks;
     h->commit_slots = (int)commit_slots;
-    h->commit_blocks = commit_blocks_for(h->slots, h->commit_slots);
+    {
+        const int rc = commit_grid(h, h->commit_slots, &h->commit_blocks);
+        if (rc) return rc;
+    }
     destroy_graphs(h);  // they bake the launch shapes in
     return EPI_OK;
 }
@@ -1027,6 +1173,7 @@ static int autotune(epi_engine* h, uint32_t hours, epi_launch_shape* out) {
         const uint32_t v = (uint32_t)std::max<uint64_t>(1, std::min<uint64_t>(g, n_chunks));
         if (std::find(grids.begin(), grids.end(), v) == grids.end()) grids.push_back(v);
     }
+    const uint32_t slot_cands[3] = {1u, 2u, 4u};
     const bool prof = h->profiling;
     const uint64_t launched = h->kernels_launched;
     h->profiling = false;
@@ -1035,8 +1182,7 @@ static int autotune(epi_engine* h, uint32_t hours, epi_launch_shape* out) {
     double best = 1e300;
     uint32_t best_g = (uint32_t)h->grid_blocks, best_c = (uint32_t)h->commit_slots;
     for (uint32_t g : grids) {
-        const uint32_t slots[3] = {1u, 2u, 4u};
-        for (uint32_t c : slots) {
+        for (uint32_t c : slot_cands) {
             rc = set_launch_shape(h, g, c);
             double t_min = 1e300;
             for (int rep = 0; rep < 3 && !rc; ++rep) {  // the first pass captures the graphs
@@ -1579,8 +1725,8 @@ namespace {
 
 constexpr size_t kNoAllocScratchBytes = size_t(48) << 20;  // 48 MiB
 constexpr size_t kNoAllocParamsOff = 0;                     // DevParams
-constexpr size_t kNoAllocHourOff = 256;                     // u32 hour
-constexpr size_t kNoAllocErrOff = 260;                      // int error flags
+constexpr size_t kNoAllocHourOff = 256;                     // SegDev {hour, hour}
+constexpr size_t kNoAllocErrOff = 264;                      // int error flags
 constexpr size_t kNoAllocTgtOff = 512;                      // u32 per agent
 static_assert(sizeof(DevParams) <= kNoAllocHourOff, "parameter block must fit its slot");
 
@@ -1662,13 +1808,15 @@ extern "C" int epi_tick_hour_noalloc(const epi_params* params, uint32_t hour, ui
     cudaStream_t s = static_cast<cudaStream_t>(cuda_stream);
     const DevParams hp = noalloc_params(*params, hospital_grown);
     DevParams* d_params = reinterpret_cast<DevParams*>(d->base + kNoAllocParamsOff);
-    uint32_t* d_hour = reinterpret_cast<uint32_t*>(d->base + kNoAllocHourOff);
+    SegDev* d_hour = reinterpret_cast<SegDev*>(d->base + kNoAllocHourOff);
+    const SegDev seg{hour, hour};
+    const HourArgs ha{d_hour, counts, 8u, 0u, 0u};
     int* d_err = reinterpret_cast<int*>(d->base + kNoAllocErrOff);
     uint32_t* d_tgt = reinterpret_cast<uint32_t*>(d->base + kNoAllocTgtOff);
     uint32_t* d_claim = reinterpret_cast<uint32_t*>(d->base + claim_off);
     // every call starts from clean scratch: the claim plane free, the error word zero
     NOALLOC_CK(cudaMemcpyAsync(d_params, &hp, sizeof hp, cudaMemcpyHostToDevice, s));
-    NOALLOC_CK(cudaMemcpyAsync(d_hour, &hour, sizeof hour, cudaMemcpyHostToDevice, s));
+    NOALLOC_CK(cudaMemcpyAsync(d_hour, &seg, sizeof seg, cudaMemcpyHostToDevice, s));
     NOALLOC_CK(cudaMemsetAsync(d_err, 0, sizeof(int), s));
     NOALLOC_CK(cudaMemsetAsync(counts, 0, 8 * sizeof(uint32_t), s));
     uint2* st = reinterpret_cast<uint2*>(state);
@@ -1676,14 +1824,14 @@ extern "C" int epi_tick_hour_noalloc(const epi_params* params, uint32_t hour, ui
     const int blocks = (int)std::min<uint64_t>(n_chunks, (uint64_t)d->grid_blocks);
     const uint32_t hod = hour % 24u;
     if (hod >= 1u && hod <= 6u) {
-        k_sleep<<<blocks, kThreads, 0, s>>>(d_params, nullptr, n_chunks, st, counts, nullptr);
+        k_sleep<<<blocks, kThreads, 0, s>>>(d_params, nullptr, n_chunks, st, ha);
     } else {
         NOALLOC_CK(cudaMemsetAsync(d_claim, 0xFF, claim_bytes, s));
         const DecideKernel decide = decide_kernel(hod);
         decide<<<blocks, kThreads, 0, s>>>(d_params, nullptr, n_chunks, pos, st, home, work, work_start_at, plane, nullptr,
-                                           d_claim, d_tgt, nullptr, counts, d_hour, 0u, d_err, nullptr);
+                                           d_claim, d_tgt, nullptr, ha, d_err);
         k_commit<kCommitSlots><<<commit_blocks_for(n), kThreads, 0, s>>>(d_params, nullptr, n, pos, d_tgt, plane, nullptr,
-                                                                         d_claim, nullptr, d_hour, 0u, nullptr);
+                                                                         d_claim, nullptr, ha, 0ull);
     }
     NOALLOC_CK(cudaGetLastError());
     int err = 0;

@@ -101,7 +101,14 @@ struct DevParams {
     uint32_t active;            // 0 once the run of this replicate has ended
     uint64_t plane_off;         // byte offset of its bordered plane
     uint64_t claim_off;         // word offset of its claim plane
+    // day-boundary guard of the run loop: the data-dependent intervention triggers still armed
+    uint32_t guard_flags;       // kGuard* bits
+    uint32_t lock_threshold;    // lockdown when infected > this
+    uint32_t spread_threshold;  // new hospital when the day's new infections >= this
+    uint32_t occ_threshold;     // new hospital when hospitalized >= this
 };
+
+constexpr uint32_t kGuardLock = 1u, kGuardSpread = 2u, kGuardOccupancy = 4u;
 
 constexpr uint32_t kChunk = 256;  // agent slots per chunk; replicates start on chunk boundaries
 

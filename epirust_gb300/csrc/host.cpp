@@ -4,6 +4,7 @@
 #include <sys/stat.h>
 
 #include <cerrno>
+#include <algorithm>
 #include <cmath>
 #include <cstdio>
 #include <cstring>
@@ -433,6 +434,39 @@ bool is_event_hour(const epi_params& p, uint32_t hour) {
     for (int k = 0; k < p.n_vaccinations; ++k)
         if (p.vaccination_at_hour[k] == hour) return true;
     return false;
+}
+
+uint32_t next_fixed_event(const epi_params& p, const InterventionState& st, uint32_t from) {
+    uint32_t e = 0xFFFFFFFFu;
+    for (int k = 0; k < p.n_vaccinations; ++k)
+        if (p.vaccination_at_hour[k] >= from) e = std::min(e, p.vaccination_at_hour[k]);
+    const uint64_t lift = (uint64_t)st.zero_infection_hour + 21u * 24u;  // decide_interventions' unlock hour
+    if (st.locked && lift >= from && lift < e) e = (uint32_t)lift;
+    return e;
+}
+
+GuardParams guard_params(const epi_params& p, const InterventionState& st, const epi_area& hospital) {
+    GuardParams g;
+    if (p.has_lockdown && !st.locked) {
+        g.flags |= 1u;
+        g.lock_threshold = p.lockdown_at_number_of_infections;
+    }
+    if (!st.hospital_applied) {
+        if (p.has_build_new_hospital) {
+            g.flags |= 2u;
+            g.spread_threshold = p.spread_rate_threshold;
+        }
+        if (p.hospital_occupancy_trigger > 0.0) {
+            // the same double product as decide_interventions; hospitalized >= x <=> >= ceil(x)
+            const double cells = (double)(hospital.x1 - hospital.x0 + 1) * (double)(hospital.y1 - hospital.y0 + 1);
+            const double x = std::ceil(p.hospital_occupancy_trigger * cells);
+            if (x <= 4294967295.0) {
+                g.flags |= 4u;
+                g.occ_threshold = (uint32_t)std::max(x, 0.0);
+            }
+        }
+    }
+    return g;
 }
 
 // process_interventions triggers (engine/src/allocation_map.rs:306-337):

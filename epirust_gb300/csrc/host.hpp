@@ -72,8 +72,23 @@ InterventionActions decide_interventions(const epi_params& p, InterventionState&
                                          const epi_area& hospital);
 
 // Is this hour one at which an intervention can fire (a day boundary or a vaccination
-// hour)?  Hour segments of the run loop end at these hours.
+// hour)?  The run loop calls decide_interventions at these hours.
 bool is_event_hour(const epi_params& p, uint32_t hour);
+
+// The first hour >= from at which an intervention fires whatever the counts are -- a
+// vaccination hour, or the lifting of a lockdown in force -- or 0xFFFFFFFF.  The run loop's
+// chains end there; the data-dependent triggers are watched on the device (GuardParams).
+uint32_t next_fixed_event(const epi_params& p, const InterventionState& st, uint32_t from);
+
+// The data-dependent triggers of decide_interventions still armed, for the device guard:
+// lockdown when infected > lock_threshold; a new hospital when the day's new infections >=
+// spread_threshold or hospitalized >= occ_threshold (the smallest count meeting the
+// occupancy fraction of the current hospital's cells).
+struct GuardParams {
+    uint32_t flags = 0;  // bit 0 lockdown, bit 1 spread, bit 2 occupancy
+    uint32_t lock_threshold = 0, spread_threshold = 0, occ_threshold = 0;
+};
+GuardParams guard_params(const epi_params& p, const InterventionState& st, const epi_area& hospital);
 
 // CsvListener + InterventionReporter output files.
 int write_outputs(const std::string& dir, const std::string& engine_id, const std::vector<epi_counts>& rows,

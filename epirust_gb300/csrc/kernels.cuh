@@ -23,6 +23,14 @@ namespace kern {
 
 constexpr int kThreads = (int)kChunk;
 
+// Programmatic dependent launch: the hour kernels are launched so that the next kernel's
+// launch is set up while the one before it runs.  dep_wait() returns once every earlier
+// kernel of the stream has completed and its writes are visible (a no-op for a normal
+// launch), so each hour kernel calls it before its first global access.  The kernels signal
+// nothing early: blocks of the next kernel resident (and waiting) beside the running one were
+// measured 1.7 % slower per hour than letting them start at its completion.
+__device__ __forceinline__ void dep_wait() { asm volatile("griddepcontrol.wait;" ::: "memory"); }
+
 // Warp-aggregated 6-bin histogram into shared memory: three ballots carry the bits of each
 // lane's bin (invalid lanes vote bin 7), and lane b (< 6) counts the lanes whose bits spell b.
 __device__ __forceinline__ void count_into(uint32_t* sh, bool valid, uint32_t bin) {
@@ -42,14 +50,43 @@ struct BlockRep {
     uint32_t r = 0xFFFFFFFFu;
 };
 
+// Hours run in chains of captured pieces (a piece ends at a day boundary) launched back to
+// back; the chain's counts rows are [hour - first][replicate][8], words 0-5 the bins and
+// word 6 the halt mark of the run loop's guard.  The hour of a launch is read on the device,
+// so one captured piece serves every day.
+struct SegDev {
+    uint32_t hour_base;  // first hour of the piece now running (advanced by k_piece_end)
+    uint32_t first;      // first hour of the chain
+};
+struct HourArgs {
+    SegDev* seg;
+    uint32_t* counts;    // the chain's rows
+    uint32_t row_words;  // R * 8
+    uint32_t offset;     // hour within the piece
+    uint32_t prev_back;  // hours back to the previous computed row (0: the stop rule is off)
+};
+struct HourRows {
+    uint32_t hour;
+    uint32_t* rows;
+    const uint32_t* prev;  // nullptr for the first hour of a chain and outside the run loop
+};
+__device__ __forceinline__ HourRows hour_rows(const HourArgs& a) {
+    HourRows o;
+    o.hour = a.seg->hour_base + a.offset;
+    const uint32_t row = o.hour - a.seg->first;
+    o.rows = a.counts + (size_t)row * a.row_words;
+    o.prev = (a.prev_back && row >= a.prev_back) ? a.counts + (size_t)(row - a.prev_back) * a.row_words : nullptr;
+    return o;
+}
+
 // The stop rule of run_single_engine (epidemiology_simulation.rs:564-575): a replicate whose
 // last computed counts row (prev, [replicate][8]) has no exposed, infected or hospitalized
-// agent has ended, and the later hours of the segment leave it untouched.  prev is nullptr
-// outside the run loop and for the first hour of a segment.
+// agent has ended, and the later hours of the chain leave it untouched; so do they after a
+// row the guard marked (an intervention fires there, and the host takes over).
 __device__ __forceinline__ bool run_ended(const uint32_t* prev, uint32_t r) {
     if (!prev) return false;
     const uint32_t* c = prev + (size_t)r * 8u;
-    return (c[1] | c[2] | c[3]) == 0u;
+    return (c[1] | c[2] | c[3]) == 0u || c[6] != 0u;
 }
 
 // Switch the block to replicate r: flush the histogram of the previous one into its counts
@@ -94,15 +131,22 @@ __device__ uint32_t block_first_vacant(const DevParams& P, const PlaneView& pl) 
 
 // Hours 1..6 (SLEEP_START_TIME..=SLEEP_END_TIME, citizen/mod.rs:244-248).
 __global__ void __launch_bounds__(kThreads) k_sleep(const DevParams* __restrict__ Pall, const uint32_t* __restrict__ chunk_rep,
-                                                    uint32_t n_chunks, uint2* __restrict__ st, uint32_t* __restrict__ counts,
-                                                    const uint32_t* __restrict__ prev) {
+                                                    uint32_t n_chunks, uint2* __restrict__ st, HourArgs ha) {
     __shared__ uint32_t sh[8];
     __shared__ DevParams sP;
+    dep_wait();
+    const HourRows hr = hour_rows(ha);
+    uint32_t* counts = hr.rows;
+    const uint32_t* prev = hr.prev;
     BlockRep br;
+    bool ended = false;  // run_ended of the block's replicate (its prev row is fixed during the launch)
     for (uint32_t c = blockIdx.x; c < n_chunks; c += gridDim.x) {
         const uint32_t r = chunk_rep ? chunk_rep[c] : 0u;
-        if (r != br.r) switch_rep(br, r, Pall, sP, sh, counts);
-        if (!sP.active || run_ended(prev, r)) continue;
+        if (r != br.r) {
+            switch_rep(br, r, Pall, sP, sh, counts);
+            ended = run_ended(prev, r);
+        }
+        if (!sP.active || ended) continue;
         const uint32_t slot = c * kChunk + threadIdx.x;
         const bool valid = slot - sP.agent_off < sP.n;
         uint32_t s = 0;
@@ -126,24 +170,27 @@ __global__ void __launch_bounds__(kThreads) k_decide(const DevParams* __restrict
                                                      const uint32_t* __restrict__ work, uint32_t* __restrict__ wsa,
                                                      const uint8_t* __restrict__ plane, const uint8_t* __restrict__ danger,
                                                      uint32_t* __restrict__ claim, uint32_t* __restrict__ tgt,
-                                                     uint32_t* __restrict__ lost, uint32_t* __restrict__ counts,
-                                                     const uint32_t* __restrict__ hour_base, uint32_t hour_offset,
-                                                     int* err, const uint32_t* __restrict__ prev) {
+                                                     uint32_t* __restrict__ lost, HourArgs ha, int* err) {
     __shared__ uint32_t sh[8];
     __shared__ DevParams sP;
     const DevParams& P = sP;
-    const uint32_t hour = *hour_base + hour_offset;
+    dep_wait();
+    const HourRows hr = hour_rows(ha);
+    uint32_t* counts = hr.rows;
+    const uint32_t* prev = hr.prev;
+    const uint32_t hour = hr.hour;
     const uint32_t hod = hour % 24u;
     BlockRep br;
     uint32_t hosp_first = kNoAction;
-    bool hosp_known = false;
+    bool hosp_known = false, ended = false;
     for (uint32_t c = blockIdx.x; c < n_chunks; c += gridDim.x) {
         const uint32_t r = chunk_rep ? chunk_rep[c] : 0u;
         if (r != br.r) {
             switch_rep(br, r, Pall, sP, sh, counts);
             hosp_known = false;
+            ended = run_ended(prev, r);  // prev is an earlier row: fixed during the launch
         }
-        if (!P.active || run_ended(prev, r)) continue;
+        if (!P.active || ended) continue;
         const PlaneView pl{plane + P.plane_off, P.G, P.WP, err, danger ? danger + P.plane_off : nullptr};
         uint32_t* rclaim = claim + P.claim_off;
         const uint32_t slot = c * kChunk + threadIdx.x;
@@ -224,82 +271,132 @@ __global__ void __launch_bounds__(kThreads) k_decide(const DevParams* __restrict
 // Resolve the claims of the hour: the lowest index that claimed a cell moves there
 // (the serial resolve of allocation_map.rs:93-102 in index order), others keep their cell.
 // With loss marks (lost != nullptr) a mover wins unless k_decide marked it beaten this
-// hour; without them the winner is read from the claim plane.  Each thread takes
-// S slots a block-width apart (S chosen by the launch-shape autotuner), issuing all their
-// independent loads first.
-constexpr int kCommitSlots = 4;  // default S
+// hour; without them the winner is read from the claim plane.  Each thread takes S slots a
+// block-width apart (S chosen by the launch-shape autotuner), issuing all their independent
+// loads first; the grid covers every slot once (a grid-stride loop here measured 1 % slower).
+constexpr int kCommitSlots = 4;   // default S
+constexpr int kMaxCommitSlots = 8;
 
 template <int S>
 __global__ void __launch_bounds__(kThreads) k_commit(const DevParams* __restrict__ Pall, const uint32_t* __restrict__ chunk_rep,
                                                      uint32_t n_slots, uint32_t* __restrict__ pos,
                                                      const uint32_t* __restrict__ tgt, uint8_t* __restrict__ plane,
-                                                     uint8_t* __restrict__ danger, const uint32_t* __restrict__ claim,
-                                                     const uint32_t* __restrict__ lost,
-                                                     const uint32_t* __restrict__ hour_base, uint32_t hour_offset,
-                                                     const uint32_t* __restrict__ prev) {
-    const uint32_t hour = *hour_base + hour_offset;
-    const uint32_t base = blockIdx.x * (blockDim.x * S) + threadIdx.x;
+                                                     uint8_t* __restrict__ danger, uint32_t* __restrict__ claim,
+                                                     const uint32_t* __restrict__ lost, HourArgs ha, uint64_t clear_cells) {
+    dep_wait();
+    const HourRows hr = hour_rows(ha);
+    const uint32_t* prev = hr.prev;
+    const uint32_t hour = hr.hour;
     // a single world's parameters once per thread; an ensemble looks each slot's replicate up
     const bool one = chunk_rep == nullptr;
     const uint32_t active0 = one ? Pall[0].active : 0u, off0 = one ? Pall[0].agent_off : 0u;
     const uint32_t wp0 = one ? (uint32_t)Pall[0].WP : 0u;
     const bool ended0 = one && run_ended(prev, 0u);
-    uint32_t t[S], p[S], l[S];
+    {
+        const uint32_t base = blockIdx.x * (blockDim.x * S) + threadIdx.x;
+        uint32_t t[S], p[S], l[S];
 #pragma unroll
-    for (int k = 0; k < S; ++k) {
-        const uint32_t slot = base + k * blockDim.x;
-        t[k] = slot < n_slots ? tgt[slot] : kNoAction;
-        p[k] = slot < n_slots ? pos[slot] : 0u;
-        l[k] = lost && slot < n_slots ? lost[slot] : 0u;
-    }
-#pragma unroll
-    for (int k = 0; k < S; ++k) {
-        if (t[k] == kNoAction) continue;
-        const uint32_t slot = base + k * blockDim.x;
-        uint32_t r = 0u, active = active0, off = off0, WP = wp0;
-        uint64_t plane_off = 0u;
-        bool ended = ended0;
-        if (!one) {
-            r = chunk_rep[slot / kChunk];
-            const DevParams& P = Pall[r];
-            active = P.active;
-            off = P.agent_off;
-            WP = (uint32_t)P.WP;
-            plane_off = P.plane_off;
-            ended = run_ended(prev, r);
+        for (int k = 0; k < S; ++k) {
+            const uint32_t slot = base + k * blockDim.x;
+            t[k] = slot < n_slots ? tgt[slot] : kNoAction;
+            p[k] = slot < n_slots ? pos[slot] : 0u;
+            l[k] = lost && slot < n_slots ? lost[slot] : 0u;
         }
-        if (!active || ended) continue;
-        const uint32_t xy = target_xy(t[k]), cls = target_class(t[k]), cls0 = target_old_class(t[k]);
-        bool win = false;
-        if (xy != p[k]) {
-            if (lost) {
-                win = l[k] != hour;
-            } else {
+#pragma unroll
+        for (int k = 0; k < S; ++k) {
+            if (t[k] == kNoAction) continue;
+            const uint32_t slot = base + k * blockDim.x;
+            uint32_t r = 0u, active = active0, off = off0, WP = wp0;
+            uint64_t plane_off = 0u;
+            bool ended = ended0;
+            if (!one) {
+                r = chunk_rep[slot / kChunk];
                 const DevParams& P = Pall[r];
-                win = claim[P.claim_off + (size_t)unpack_y(xy) * (uint32_t)P.W + unpack_x(xy)] ==
-                      claim_key(hour, slot - off);
+                active = P.active;
+                off = P.agent_off;
+                WP = (uint32_t)P.WP;
+                plane_off = P.plane_off;
+                ended = run_ended(prev, r);
+            }
+            if (!active || ended) continue;
+            const uint32_t xy = target_xy(t[k]), cls = target_class(t[k]), cls0 = target_old_class(t[k]);
+            bool win = false;
+            if (xy != p[k]) {
+                if (lost) {
+                    win = l[k] != hour;
+                } else {
+                    const DevParams& P = Pall[r];
+                    win = claim[P.claim_off + (size_t)unpack_y(xy) * (uint32_t)P.W + unpack_x(xy)] ==
+                          claim_key(hour, slot - off);
+                }
+            }
+            uint8_t* rplane = plane + plane_off;
+            const size_t old_cell = (size_t)(unpack_y(p[k]) + 1) * WP + (unpack_x(p[k]) + 1);
+            size_t new_cell = old_cell;
+            if (win) {
+                new_cell = (size_t)(unpack_y(xy) + 1) * WP + (unpack_x(xy) + 1);
+                rplane[old_cell] = 0;
+                rplane[new_cell] = (uint8_t)cls;
+                pos[slot] = xy;
+            } else {
+                rplane[old_cell] = (uint8_t)cls;
+            }
+            // infectious-neighbour counts follow infectious agents that move or stop or start
+            // being infectious (rare: a few agents per hour)
+            const bool inf0 = cls0 >= 2u, inf1 = cls >= 2u;
+            if (danger && (inf0 || inf1) && (inf0 != inf1 || new_cell != old_cell)) {
+                uint8_t* rd = danger + plane_off;
+                if (inf0) danger_add(rd, old_cell, WP, -1);
+                if (inf1) danger_add(rd, new_cell, WP, +1);
             }
         }
-        uint8_t* rplane = plane + plane_off;
-        const size_t old_cell = (size_t)(unpack_y(p[k]) + 1) * WP + (unpack_x(p[k]) + 1);
-        size_t new_cell = old_cell;
-        if (win) {
-            new_cell = (size_t)(unpack_y(xy) + 1) * WP + (unpack_x(xy) + 1);
-            rplane[old_cell] = 0;
-            rplane[new_cell] = (uint8_t)cls;
-            pos[slot] = xy;
-        } else {
-            rplane[old_cell] = (uint8_t)cls;
-        }
-        // infectious-neighbour counts follow infectious agents that move or stop or start
-        // being infectious (rare: a few agents per hour)
-        const bool inf0 = cls0 >= 2u, inf1 = cls >= 2u;
-        if (danger && (inf0 || inf1) && (inf0 != inf1 || new_cell != old_cell)) {
-            uint8_t* rd = danger + plane_off;
-            if (inf0) danger_add(rd, old_cell, WP, -1);
-            if (inf1) danger_add(rd, new_cell, WP, +1);
-        }
     }
+    // A new claim window (kClaimWindow hours) opens before the next hour that claims (hour of
+    // day 0 claims next at 7): every claim plane is reset for it.  Only with loss marks, where
+    // this kernel reads no claim.
+    if (clear_cells && lost) {
+        const uint32_t next = hour % 24u == 0u ? hour + 7u : hour + 1u;
+        if (next / kClaimWindow != hour / kClaimWindow)
+            for (size_t i = (size_t)blockIdx.x * blockDim.x + threadIdx.x; i < clear_cells; i += (size_t)gridDim.x * blockDim.x)
+                claim[i] = kNoClaim;
+    }
+}
+
+// End of a piece: the run loop's guard at a day boundary (row `guard_offset` of the piece;
+// kNoGuard for none), then the piece's hours are added to the chain's hour base.  The guard
+// evaluates the data-dependent triggers of process_interventions -- lockdown when infected >
+// its threshold, a new hospital when the day's new infections (infected minus the previous
+// boundary's figure, floored at 0) reach the spread threshold or hospitalized reaches the
+// occupancy threshold -- for every replicate whose row ran, keeping the new-infections figure
+// per replicate in ivn; if any fires, the row of every replicate gets the halt mark, and the
+// rest of the chain does nothing.  One block.
+constexpr uint32_t kNoGuard = 0xFFFFFFFFu;
+
+__global__ void k_piece_end(const DevParams* __restrict__ Pall, uint32_t R, SegDev* seg, uint32_t* counts,
+                            uint32_t row_words, uint32_t guard_offset, uint32_t advance, uint32_t* __restrict__ ivn) {
+    __shared__ int fire;
+    if (threadIdx.x == 0) fire = 0;
+    __syncthreads();
+    if (guard_offset != kNoGuard) {
+        uint32_t* rows = counts + (size_t)(seg->hour_base + guard_offset - seg->first) * row_words;
+        for (uint32_t r = threadIdx.x; r < R; r += blockDim.x) {
+            const DevParams& P = Pall[r];
+            const uint32_t* c = rows + (size_t)r * 8u;
+            if (!P.active || (c[0] | c[1] | c[2] | c[3] | c[4] | c[5]) == 0u) continue;  // the hour did not run
+            const uint32_t infected = c[2], hospitalized = c[3];
+            const uint32_t fresh = infected > ivn[r] ? infected - ivn[r] : 0u;
+            ivn[r] = fresh;
+            const bool f = ((P.guard_flags & kGuardLock) && infected > P.lock_threshold) ||
+                           ((P.guard_flags & kGuardSpread) && fresh >= P.spread_threshold) ||
+                           ((P.guard_flags & kGuardOccupancy) && hospitalized >= P.occ_threshold);
+            if (f) fire = 1;
+        }
+        __syncthreads();
+        if (fire)
+            for (uint32_t r = threadIdx.x; r < R; r += blockDim.x) rows[(size_t)r * 8u + 6u] = 1u;
+    }
+    __syncthreads();
+    if (advance && threadIdx.x == 0) seg->hour_base += advance;
 }
 
 // Plane bytes of every agent of every replicate (world upload).

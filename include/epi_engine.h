@@ -268,10 +268,10 @@ int epi_engine_restore_state(epi_engine* h);
 int epi_engine_kernels_launched(const epi_engine* h, uint64_t* out);
 
 /* Launch shape of the tick kernels: the k_decide / k_sleep grid and the agents per k_commit
- * thread.  Results never depend on it. */
+ * thread (its grid covers every agent once).  Results never depend on it. */
 typedef struct {
     uint32_t decide_blocks;  /* 1 .. number of 256-agent chunks */
-    uint32_t commit_slots;   /* 1, 2 or 4 */
+    uint32_t commit_slots;   /* 1 .. 8 */
     double hour_us;          /* autotune: mean wall time of a simulated hour with this shape */
 } epi_launch_shape;
 

@@ -266,5 +266,5 @@ def test_profiling_counts_kernels(gpu):
     stats = eng.kernel_stats()
     # hours 2..6 repeat hour 1 within a segment: one sleep launch per day
     assert stats["k_sleep"][0] == 1 and stats["k_decide"][0] == 18 and stats["k_commit"][0] == 18
-    assert eng.kernels_launched() - before == 1 + 2 * 18
+    assert eng.kernels_launched() - before == 1 + 2 * 18 + 1  # and the piece end (k_piece_end)
     assert all(ms > 0 for launches, ms in stats.values() if launches)

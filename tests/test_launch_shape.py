@@ -1,5 +1,5 @@
 """Launch shapes and the autotuner: the tick's results never depend on the k_decide grid or
-the agents per k_commit thread, and autotuning leaves the world where it found it."""
+the agents per k_commit thread (1..8), and autotuning leaves the world where it found it."""
 import json
 
 import numpy as np
@@ -25,7 +25,7 @@ def test_every_launch_shape_gives_the_same_hours(gpu, oracle_mod):
     sim = oracle_mod.O1(oracle_mod.params_from_config(cfg))
     want = rows_to_array(sim.run(1, 130, interventions=False, stop=False))
     n_chunks = (6000 + 255) // 256
-    for blocks, slots in [(None, None), (n_chunks, 1), (1, 2), (7, 4)]:
+    for blocks, slots in [(None, None), (n_chunks, 1), (1, 2), (7, 4), (3, 5), (n_chunks, 8), (2, 3)]:
         eng = _engine(cfg)
         if blocks:
             eng.set_launch_shape(blocks, slots)
@@ -41,7 +41,7 @@ def test_bad_launch_shapes_are_refused(gpu):
     from epirust_gb300 import EpiError
 
     eng = _engine(make_config(n=3000, grid=120, seed=1))
-    for blocks, slots in [(0, 4), (10**6, 4), (4, 3)]:
+    for blocks, slots in [(0, 4), (10**6, 4), (4, 0), (4, 9)]:
         with pytest.raises(EpiError, match="ARG"):
             eng.set_launch_shape(blocks, slots)
     eng.close()
@@ -54,7 +54,7 @@ def test_autotune_keeps_the_world_and_the_run(gpu, oracle_mod):
     before = eng.snapshot().copy()
     launched = eng.kernels_launched()
     shape = eng.autotune(24)
-    assert shape["commit_slots"] in (1, 2, 4) and shape["decide_blocks"] >= 1 and shape["hour_us"] > 0
+    assert 1 <= shape["commit_slots"] <= 8 and shape["decide_blocks"] >= 1 and shape["hour_us"] > 0
     assert eng.launch_shape() == {"decide_blocks": shape["decide_blocks"], "commit_slots": shape["commit_slots"]}
     assert (eng.snapshot().view(np.uint8) == before.view(np.uint8)).all()
     assert eng.kernels_launched() == launched
@@ -71,7 +71,7 @@ def test_ensemble_autotune_keeps_replicates_equal_to_single_engines(gpu):
             for i, (n, g) in enumerate([(2000, 100), (700, 60), (4100, 120)])]
     ens = Ensemble([Config(json.dumps(c)).params for c in cfgs])
     shape = ens.autotune(12)
-    assert shape["commit_slots"] in (1, 2, 4)
+    assert 1 <= shape["commit_slots"] <= 8
     rows = ens.run()
     for c, r in zip(cfgs, rows):
         eng = _engine(c)
