@@ -324,16 +324,19 @@ static bool sleep_hour_skipped(uint32_t first_hour, uint32_t k) {
 }
 
 // The k_decide instance of an hour of the day.
-static DecideKernel decide_kernel(uint32_t hod) {
+// The k_decide (single world) or k_decide_ens (ensemble) instance of an hour of the day.
+static DecideKernel decide_kernel(uint32_t hod, bool ensemble = false) {
+#define EPI_PICK(HC) (ensemble ? (DecideKernel)k_decide_ens<HC> : (DecideKernel)k_decide<HC>)
     switch (hour_class(hod)) {
-        case kHcStart: return k_decide<kHcStart>;
-        case kHcEnd: return k_decide<kHcEnd>;
-        case kHcTransport: return k_decide<kHcTransport>;
-        case kHcWork: return k_decide<kHcWork>;
-        case kHcNoon: return k_decide<kHcNoon>;
-        case kHcHome: return k_decide<kHcHome>;
-        default: return k_decide<kHcMove>;
+        case kHcStart: return EPI_PICK(kHcStart);
+        case kHcEnd: return EPI_PICK(kHcEnd);
+        case kHcTransport: return EPI_PICK(kHcTransport);
+        case kHcWork: return EPI_PICK(kHcWork);
+        case kHcNoon: return EPI_PICK(kHcNoon);
+        case kHcHome: return EPI_PICK(kHcHome);
+        default: return EPI_PICK(kHcMove);
     }
+#undef EPI_PICK
 }
 
 static int commit_blocks_for(uint32_t slots, int per_thread = kCommitSlots) {
@@ -392,7 +395,7 @@ static int enqueue_piece(epi_engine* h, uint32_t first_hour, uint32_t nh) {
             LAUNCH(kKSleep, CK(launch_hour_kernel(k_sleep, h->grid_blocks, h->stream, (const DevParams*)h->d_params,
                                                   (const uint32_t*)h->d_chunk_rep, n_chunks, h->d_st, ha)));
         } else {
-            const DecideKernel decide = decide_kernel(hod);
+            const DecideKernel decide = decide_kernel(hod, h->R() > 1);
             LAUNCH(kKDecide, CK(launch_hour_kernel(
                                   decide, h->grid_blocks, h->stream, (const DevParams*)h->d_params,
                                   (const uint32_t*)h->d_chunk_rep, n_chunks, (const uint32_t*)h->d_pos, h->d_st,
@@ -984,7 +987,7 @@ static int engine_init(epi_engine* h, const epi_params* params, const epi_agent_
     int dev = 0, sms = 0, per_sm = 0;
     CK(cudaGetDevice(&dev));
     CK(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev));
-    CK(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_decide<kHcMove>, kThreads, 0));
+    CK(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, (const void*)decide_kernel(9u, R > 1), kThreads, 0));
     per_sm = std::max(per_sm, 1);
     const uint64_t n_chunks = slots / kChunk;
     h->resident_blocks = sms * per_sm;
@@ -1771,7 +1774,7 @@ int noalloc_setup(int dev, NoAllocDevice** out) {
         NOALLOC_CK(cudaGetSymbolAddress(&ptr, g_noalloc_scratch));
         int sms = 0, per_sm = 0;
         NOALLOC_CK(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev));
-        NOALLOC_CK(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_decide<kHcMove>, kThreads, 0));
+        NOALLOC_CK(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, (const void*)decide_kernel(9u), kThreads, 0));
         d.grid_blocks = sms * std::max(per_sm, 1);
         d.base = static_cast<unsigned char*>(ptr);
     }

@@ -65,18 +65,21 @@ struct HourArgs {
     uint32_t offset;     // hour within the piece
     uint32_t prev_back;  // hours back to the previous computed row (0: the stop rule is off)
 };
-struct HourRows {
-    uint32_t hour;
-    uint32_t* rows;
-    const uint32_t* prev;  // nullptr for the first hour of a chain and outside the run loop
+// The hour of a launch and its row in the chain.  The row pointers are recomputed where they
+// are used (from kernel parameters) rather than held in registers across the kernel.
+struct HourRow {
+    uint32_t hour, row;
 };
-__device__ __forceinline__ HourRows hour_rows(const HourArgs& a) {
-    HourRows o;
-    o.hour = a.seg->hour_base + a.offset;
-    const uint32_t row = o.hour - a.seg->first;
-    o.rows = a.counts + (size_t)row * a.row_words;
-    o.prev = (a.prev_back && row >= a.prev_back) ? a.counts + (size_t)(row - a.prev_back) * a.row_words : nullptr;
-    return o;
+__device__ __forceinline__ HourRow hour_row(const HourArgs& a) {
+    const uint32_t hour = a.seg->hour_base + a.offset;
+    return HourRow{hour, hour - a.seg->first};
+}
+__device__ __forceinline__ uint32_t* row_ptr(const HourArgs& a, uint32_t row) {
+    return a.counts + (size_t)row * a.row_words;
+}
+// The previous computed row: nullptr for the first hour of a chain and outside the run loop.
+__device__ __forceinline__ const uint32_t* prev_ptr(const HourArgs& a, uint32_t row) {
+    return (a.prev_back && row >= a.prev_back) ? a.counts + (size_t)(row - a.prev_back) * a.row_words : nullptr;
 }
 
 // The stop rule of run_single_engine (epidemiology_simulation.rs:564-575): a replicate whose
@@ -135,16 +138,14 @@ __global__ void __launch_bounds__(kThreads) k_sleep(const DevParams* __restrict_
     __shared__ uint32_t sh[8];
     __shared__ DevParams sP;
     dep_wait();
-    const HourRows hr = hour_rows(ha);
-    uint32_t* counts = hr.rows;
-    const uint32_t* prev = hr.prev;
+    const HourRow hr = hour_row(ha);
     BlockRep br;
     bool ended = false;  // run_ended of the block's replicate (its prev row is fixed during the launch)
     for (uint32_t c = blockIdx.x; c < n_chunks; c += gridDim.x) {
         const uint32_t r = chunk_rep ? chunk_rep[c] : 0u;
         if (r != br.r) {
-            switch_rep(br, r, Pall, sP, sh, counts);
-            ended = run_ended(prev, r);
+            switch_rep(br, r, Pall, sP, sh, row_ptr(ha, hr.row));
+            ended = run_ended(prev_ptr(ha, hr.row), r);
         }
         if (!sP.active || ended) continue;
         const uint32_t slot = c * kChunk + threadIdx.x;
@@ -159,25 +160,30 @@ __global__ void __launch_bounds__(kThreads) k_sleep(const DevParams* __restrict_
         }
         count_into(sh, valid, count_bin(s));
     }
-    flush_rep(br, sh, counts);
+    flush_rep(br, sh, row_ptr(ha, hr.row));
 }
 
 // One hour of per-agent rules (hour of day 0, 7..22 or 23), specialised per hour class HC.
+// The body is shared by two kernels that differ only in their launch bounds: k_decide for a
+// single world (registers left to the compiler: 55 for the movement classes) and
+// k_decide_ens for ensembles (at least kEnsembleMinBlocks resident blocks: 48 registers),
+// whose per-chunk replicate switches favour occupancy; each was measured faster on its own
+// workload.
+constexpr int kEnsembleMinBlocks = 5;
+
 template <int HC>
-__global__ void __launch_bounds__(kThreads) k_decide(const DevParams* __restrict__ Pall, const uint32_t* __restrict__ chunk_rep,
-                                                     uint32_t n_chunks, const uint32_t* __restrict__ pos,
-                                                     uint2* __restrict__ st, const uint32_t* __restrict__ home,
-                                                     const uint32_t* __restrict__ work, uint32_t* __restrict__ wsa,
-                                                     const uint8_t* __restrict__ plane, const uint8_t* __restrict__ danger,
-                                                     uint32_t* __restrict__ claim, uint32_t* __restrict__ tgt,
-                                                     uint32_t* __restrict__ lost, HourArgs ha, int* err) {
+__device__ __forceinline__ void decide_body(const DevParams* __restrict__ Pall, const uint32_t* __restrict__ chunk_rep,
+                                            uint32_t n_chunks, const uint32_t* __restrict__ pos, uint2* __restrict__ st,
+                                            const uint32_t* __restrict__ home, const uint32_t* __restrict__ work,
+                                            uint32_t* __restrict__ wsa, const uint8_t* __restrict__ plane,
+                                            const uint8_t* __restrict__ danger, uint32_t* __restrict__ claim,
+                                            uint32_t* __restrict__ tgt, uint32_t* __restrict__ lost, const HourArgs& ha,
+                                            int* err) {
     __shared__ uint32_t sh[8];
     __shared__ DevParams sP;
     const DevParams& P = sP;
     dep_wait();
-    const HourRows hr = hour_rows(ha);
-    uint32_t* counts = hr.rows;
-    const uint32_t* prev = hr.prev;
+    const HourRow hr = hour_row(ha);
     const uint32_t hour = hr.hour;
     const uint32_t hod = hour % 24u;
     BlockRep br;
@@ -186,9 +192,9 @@ __global__ void __launch_bounds__(kThreads) k_decide(const DevParams* __restrict
     for (uint32_t c = blockIdx.x; c < n_chunks; c += gridDim.x) {
         const uint32_t r = chunk_rep ? chunk_rep[c] : 0u;
         if (r != br.r) {
-            switch_rep(br, r, Pall, sP, sh, counts);
+            switch_rep(br, r, Pall, sP, sh, row_ptr(ha, hr.row));
             hosp_known = false;
-            ended = run_ended(prev, r);  // prev is an earlier row: fixed during the launch
+            ended = run_ended(prev_ptr(ha, hr.row), r);  // an earlier row: fixed during the launch
         }
         if (!P.active || ended) continue;
         const PlaneView pl{plane + P.plane_off, P.G, P.WP, err, danger ? danger + P.plane_off : nullptr};
@@ -265,8 +271,24 @@ __global__ void __launch_bounds__(kThreads) k_decide(const DevParams* __restrict
         }
         count_into(sh, valid, bin);
     }
-    flush_rep(br, sh, counts);
+    flush_rep(br, sh, row_ptr(ha, hr.row));
 }
+
+#define EPI_DECIDE_PARAMS                                                                                              \
+    const DevParams *__restrict__ Pall, const uint32_t *__restrict__ chunk_rep, uint32_t n_chunks,                    \
+        const uint32_t *__restrict__ pos, uint2 *__restrict__ st, const uint32_t *__restrict__ home,                  \
+        const uint32_t *__restrict__ work, uint32_t *__restrict__ wsa, const uint8_t *__restrict__ plane,             \
+        const uint8_t *__restrict__ danger, uint32_t *__restrict__ claim, uint32_t *__restrict__ tgt,                 \
+        uint32_t *__restrict__ lost, HourArgs ha, int *err
+template <int HC>
+__global__ void __launch_bounds__(kThreads) k_decide(EPI_DECIDE_PARAMS) {
+    decide_body<HC>(Pall, chunk_rep, n_chunks, pos, st, home, work, wsa, plane, danger, claim, tgt, lost, ha, err);
+}
+template <int HC>
+__global__ void __launch_bounds__(kThreads, kEnsembleMinBlocks) k_decide_ens(EPI_DECIDE_PARAMS) {
+    decide_body<HC>(Pall, chunk_rep, n_chunks, pos, st, home, work, wsa, plane, danger, claim, tgt, lost, ha, err);
+}
+#undef EPI_DECIDE_PARAMS
 
 // Resolve the claims of the hour: the lowest index that claimed a cell moves there
 // (the serial resolve of allocation_map.rs:93-102 in index order), others keep their cell.
@@ -284,8 +306,8 @@ __global__ void __launch_bounds__(kThreads) k_commit(const DevParams* __restrict
                                                      uint8_t* __restrict__ danger, uint32_t* __restrict__ claim,
                                                      const uint32_t* __restrict__ lost, HourArgs ha, uint64_t clear_cells) {
     dep_wait();
-    const HourRows hr = hour_rows(ha);
-    const uint32_t* prev = hr.prev;
+    const HourRow hr = hour_row(ha);
+    const uint32_t* prev = prev_ptr(ha, hr.row);
     const uint32_t hour = hr.hour;
     // a single world's parameters once per thread; an ensemble looks each slot's replicate up
     const bool one = chunk_rep == nullptr;
