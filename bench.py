@@ -38,6 +38,19 @@ METRIC = "agent-hours/s"
 # (G+1)^2 infectious-neighbour counts.
 DECIDE_BYTES_PER_AGENT = 32
 DECIDE_PLANES = 2
+# Whole-tick algorithmic bytes per agent-hour of the reference-layout accounting (agent record
+# read 25 B + written 11 B, claim write and clear, plane write, and the occupancy and
+# infectiousness planes amortised over the agents -- 76 B at 1M agents / 2500 grid in a
+# movement hour; 16 B at hour of day 0, 3 B in the sleep hours, 12 B at hour 23), the
+# per-unit figure of the run roofline below.
+def tick_bytes_per_agent_hour(hod: int, agents: int, grid: int) -> float:
+    if hod == 0:
+        return 16.0
+    if 1 <= hod <= 6:
+        return 3.0
+    if hod == 23:
+        return 12.0
+    return 36.0 + 8.0 + 1.0 + 5.0 * (grid + 1) ** 2 / agents
 
 
 def _peaks():
@@ -400,6 +413,10 @@ def run_gpu(args, cfg):
             first = f.readline()
         traffic = int(first.rsplit(":", 1)[1]) * n // 1_000_000  # captured at 1M agents; scales with agents
 
+    # run roofline: every simulated hour's algorithmic bytes over the timed step
+    run_bytes = sum(n * tick_bytes_per_agent_hour(h % 24, n, G) for h in range(1, hours_per_step + 1))
+    run_achieved = run_bytes / (ms_total / args.steps / 1000.0) / 1e9
+
     batched = run_batched(args, stream, flush) if not args.no_batched else None
 
     surrogate = run_surrogate(args) if rank == 0 and not args.no_surrogate else None
@@ -421,6 +438,10 @@ def run_gpu(args, cfg):
                          "alg_bytes_per_launch": alg_bytes, "avg_launch_ms": avg_ms,
                          "share_of_kernel_time": ms_d / total_kernel_ms if total_kernel_ms else None,
                          "issue": issue,
+                         "run": {"achieved": run_achieved, "peak": peak, "unit": "GB/s", "frac": run_achieved / peak,
+                                 "bytes_per_step": run_bytes,
+                                 "basis": "whole run: per agent-hour 76 B (movement hours at 1M/2500), 16 B (hour 0), "
+                                          "3 B (hours 1-6), 12 B (hour 23), reference-layout accounting"},
                          "kernels": {k: {"launches": v[0], "ms": v[1]} for k, v in stats.items() if v[0]}},
             "cpu_baseline": cpu,
             "e2e": {"value": e2e_value, "unit": METRIC, "h2d_bytes_per_step": int(n * 24),
