@@ -78,35 +78,45 @@ struct AdamHyper {
     float lr, beta1, beta2, eps;
 };
 
-// One Adam step (Kingma & Ba 2015, with bias correction) on W (N x K) and b (N) of a layer of
-// member blockIdx.y; t = *step + 1.  Writes the BF16 copies W and W^T.
-__global__ void k_adam(float* __restrict__ w, const float* __restrict__ gw, float* __restrict__ mw, float* __restrict__ vw,
-                       float* __restrict__ b, const float* __restrict__ gb, float* __restrict__ mb, float* __restrict__ vb,
-                       __nv_bfloat16* __restrict__ wb, __nv_bfloat16* __restrict__ wtb, uint32_t N, uint32_t K,
-                       const uint32_t* __restrict__ step, AdamHyper hp) {
+// One Adam step (Kingma & Ba 2015, with bias correction) of member blockIdx.y; t = *step + 1.
+// Blocks below (N / 32) * (K / 32) take a 32 x 32 tile of W (N x K; both multiples of 32) and
+// write its BF16 copies W and W^T, the transpose through shared memory so that both stores
+// are coalesced; the blocks after them take 256 entries of b each.  256 threads.
+__device__ __forceinline__ float adam_update(float* p, float* m, float* v, float g, float c1, float c2, const AdamHyper& hp) {
+    const float mi = hp.beta1 * *m + (1.f - hp.beta1) * g;
+    const float vi = hp.beta2 * *v + (1.f - hp.beta2) * g * g;
+    *m = mi;
+    *v = vi;
+    const float np = *p - hp.lr * (mi / c1) / (sqrtf(vi / c2) + hp.eps);
+    *p = np;
+    return np;
+}
+
+__global__ void __launch_bounds__(256) k_adam(float* __restrict__ w, const float* __restrict__ gw, float* __restrict__ mw,
+                                              float* __restrict__ vw, float* __restrict__ b, const float* __restrict__ gb,
+                                              float* __restrict__ mb, float* __restrict__ vb, __nv_bfloat16* __restrict__ wb,
+                                              __nv_bfloat16* __restrict__ wtb, uint32_t N, uint32_t K,
+                                              const uint32_t* __restrict__ step, AdamHyper hp) {
+    __shared__ __nv_bfloat16 tile[32][34];
     const float t = (float)(*step + 1u);
     const float c1 = 1.f - powf(hp.beta1, t), c2 = 1.f - powf(hp.beta2, t);
     const size_t nw = (size_t)N * K, ow = (size_t)blockIdx.y * nw, ob = (size_t)blockIdx.y * N;
-    w += ow; gw += ow; mw += ow; vw += ow; wb += ow; wtb += ow;
-    b += ob; gb += ob; mb += ob; vb += ob;
-    for (size_t i = (size_t)blockIdx.x * blockDim.x + threadIdx.x; i < nw + N; i += (size_t)gridDim.x * blockDim.x) {
-        const bool is_w = i < nw;
-        float* p = is_w ? w + i : b + (i - nw);
-        float* m = is_w ? mw + i : mb + (i - nw);
-        float* v = is_w ? vw + i : vb + (i - nw);
-        const float g = is_w ? gw[i] : gb[i - nw];
-        const float mi = hp.beta1 * *m + (1.f - hp.beta1) * g;
-        const float vi = hp.beta2 * *v + (1.f - hp.beta2) * g * g;
-        *m = mi;
-        *v = vi;
-        const float np = *p - hp.lr * (mi / c1) / (sqrtf(vi / c2) + hp.eps);
-        *p = np;
-        if (is_w) {
-            const __nv_bfloat16 q = __float2bfloat16_rn(np);
-            const size_t n = i / K, k = i % K;
+    const uint32_t tiles_k = K / 32u, n_tiles = N / 32u * tiles_k;
+    if (blockIdx.x < n_tiles) {
+        w += ow; gw += ow; mw += ow; vw += ow; wb += ow; wtb += ow;
+        const uint32_t n0 = blockIdx.x / tiles_k * 32u, k0 = blockIdx.x % tiles_k * 32u;
+        const uint32_t tx = threadIdx.x & 31u, ty = threadIdx.x >> 5;
+        for (uint32_t r = ty; r < 32u; r += 8u) {
+            const size_t i = (size_t)(n0 + r) * K + k0 + tx;
+            const __nv_bfloat16 q = __float2bfloat16_rn(adam_update(w + i, mw + i, vw + i, gw[i], c1, c2, hp));
             wb[i] = q;
-            wtb[k * N + n] = q;
+            tile[r][tx] = q;
         }
+        __syncthreads();
+        for (uint32_t r = ty; r < 32u; r += 8u) wtb[(size_t)(k0 + r) * N + n0 + tx] = tile[tx][r];
+    } else {
+        const uint32_t j = (blockIdx.x - n_tiles) * blockDim.x + threadIdx.x;
+        if (j < N) adam_update(b + ob + j, mb + ob + j, vb + ob + j, gb[ob + j], c1, c2, hp);
     }
 }
 
@@ -323,7 +333,8 @@ int enqueue_fwd_bwd(epi_mlp* h, float* loss) {
 int enqueue_adam(epi_mlp* h) {
     const AdamHyper hp{h->cfg.lr, h->cfg.beta1, h->cfg.beta2, h->cfg.eps};
     for (auto& ly : h->layers) {
-        k_adam<<<dim3(blocks_for((size_t)ly.N * ly.K + ly.N), h->E), kSmallThreads, 0, h->stream>>>(
+        const uint32_t blocks = ly.N / 32u * (ly.K / 32u) + (ly.N + kSmallThreads - 1) / kSmallThreads;
+        k_adam<<<dim3(blocks, h->E), kSmallThreads, 0, h->stream>>>(
             ly.w, ly.gw, ly.mw, ly.vw, ly.b, ly.gb, ly.mb, ly.vb, ly.wb, ly.wtb, ly.N, ly.K, h->d_step, hp);
         MCK(cudaGetLastError());
         h->launches++;

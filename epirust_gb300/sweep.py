@@ -34,8 +34,11 @@ def grid_for(agents: int, density: float = 0.16) -> int:
 
 def train_on_abm(runs: int = 4096, held_out: int = 512, agents: int = 100_000, days: int = 100,
                  members: int = 5, steps: int = 3000, seed: int = 4, hidden: int = 512, hidden_layers: int = 3,
-                 batch: int = 256, abm_batch: int = 512, per_agents: int = 100_000, curves: np.ndarray | None = None):
-    """curves: ABM curves of this design computed before (skips the ABM stage)."""
+                 batch: int = 256, abm_batch: int = 512, per_agents: int = 100_000, curves: np.ndarray | None = None,
+                 noise_runs: int = 128):
+    """curves: ABM curves of this design computed before (skips the ABM stage).  noise_runs
+    held-out points are simulated again with other seeds to measure the ABM's own peak-height
+    spread, the floor of any surrogate's error against single runs."""
     grid = grid_for(agents)
     hours = 24 * days + 1
     u = latin_hypercube(runs, len(PARAMS), seed)
@@ -58,6 +61,13 @@ def train_on_abm(runs: int = 4096, held_out: int = 512, agents: int = 100_000, d
     mse_net = float(np.mean((mean_pred - yte) ** 2))
     mse_mean = float(np.mean((ytr.mean(axis=0) - yte) ** 2))
     pe = relative_peak_error(mean_pred, yte, days)
+    # the ABM's own spread: held-out points run again with other seeds, peak against peak
+    n_rep = min(noise_runs, held_out)
+    t0 = time.perf_counter()
+    rep_cfgs = [config_for(d, agents, grid, hours, seed=seed * 1_000_003 + 500_000 + i, per_agents=per_agents)
+                for i, d in enumerate(denormalise(xte[:n_rep]))]
+    pe_rep = relative_peak_error(simulate_curves(rep_cfgs, days, batch=abm_batch), yte[:n_rep], days) if n_rep else None
+    t_rep = time.perf_counter() - t0
     samples = members * steps * batch
     flop = 3.0 * _flops(len(PARAMS), hidden, hidden_layers, 6 * days) * samples  # forward + backward ~ 3x forward
     info = {
@@ -68,7 +78,13 @@ def train_on_abm(runs: int = 4096, held_out: int = 512, agents: int = 100_000, d
         "final_loss": [float(l[-20:].mean()) for l in losses],
         "held_out_mse": mse_net, "mean_curve_mse": mse_mean, "gain_vs_mean_curve": mse_mean / max(mse_net, 1e-30),
         "held_out_peak_rel_err_median": float(np.median(pe)), "held_out_peak_rel_err_p90": float(np.quantile(pe, 0.9)),
+        "held_out_peak_within_5pct": float(np.mean(pe <= 0.05)),
     }
+    if pe_rep is not None:
+        info["abm_replicate_peak_rel_err"] = {
+            "runs": n_rep, "median": float(np.median(pe_rep)), "p90": float(np.quantile(pe_rep, 0.9)),
+            "within_5pct": float(np.mean(pe_rep <= 0.05)), "s": t_rep,
+            "note": "the same held-out parameters run again with other seeds: the ABM's own peak-height spread"}
     info["curves"] = y
     return net, info
 
