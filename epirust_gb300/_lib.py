@@ -109,6 +109,7 @@ EXPORTS = [
     "epi_ensemble_kernels_launched", "epi_ensemble_hour_bytes", "epi_engine_autotune", "epi_engine_set_launch_shape",
     "epi_engine_launch_shape", "epi_ensemble_autotune", "epi_engine_state_stream_open", "epi_engine_state_stream_close",
     "epi_population_read_csv", "epi_world_build_population", "epi_engine_create_population",
+    "epi_engine_run_until", "epi_engine_checkpoint_write", "epi_engine_create_from_checkpoint",
 ]
 
 
@@ -175,6 +176,9 @@ def lib():
     _sig(L, "epi_engine_vaccinate", C.c_int, [V, C.c_uint32, C.c_double])
     _sig(L, "epi_engine_increase_hospital_size", C.c_int, [V])
     _sig(L, "epi_engine_run", C.c_int, [V, V, C.c_uint32, P(C.c_uint32)])
+    _sig(L, "epi_engine_run_until", C.c_int, [V, C.c_uint32, V, C.c_uint32, P(C.c_uint32), P(C.c_uint32)])
+    _sig(L, "epi_engine_checkpoint_write", C.c_int, [V, C.c_char_p])
+    _sig(L, "epi_engine_create_from_checkpoint", C.c_int, [C.c_char_p, P(V)])
     _sig(L, "epi_engine_write_outputs", C.c_int, [V, C.c_char_p, C.c_char_p])
     _sig(L, "epi_engine_population", C.c_int, [V, P(C.c_uint32)])
     _sig(L, "epi_engine_snapshot", C.c_int, [V, V, C.c_size_t])

@@ -53,6 +53,7 @@ struct Replica {
     epi_geography s_geo{};
     uint32_t s_hosp_code = kHosp0;
     bool s_active = true;
+    std::vector<epi_counts> s_rows;
 };
 
 struct epi_engine {
@@ -103,6 +104,8 @@ struct epi_engine {
     uint64_t kernels_launched = 0;
     int64_t last_claim_hour = -1;  // latest hour whose claims may sit in the claim plane (-1: clean)
     bool stop_rule = false;        // inside the run loop: hours after a replicate's stop do nothing
+    uint32_t loop_hour = 0;        // next hour of a paused run loop (0: none in progress)
+    uint32_t s_loop_hour = 0;      // ... at the last save_state
     const uint8_t* init_flags = nullptr;  // during creation: Csv population flags of replicate 0
     // citizen-state stream (single world): per-hour codes written by k_state_delta
     FILE* stream_file = nullptr;
@@ -718,14 +721,18 @@ static int set_all_active(epi_engine* h) {
     return push_params(h);
 }
 
-static int run_loop_body(epi_engine* h);
+static int run_loop_body(epi_engine* h, uint32_t until);
 
-// Replicates drop out of the lockstep loop as their runs end; afterwards all of them are
-// active again, so that direct hour calls keep working on every world.
-static int run_loop(epi_engine* h) {
+// The run loop through hour `until` (all of it for 0xFFFFFFFF), starting at hour 1 or where a
+// paused run stopped.  Replicates drop out of the lockstep loop as their runs end; once the
+// run is over all of them are active again, so that direct hour calls keep working on every
+// world (a paused run keeps its flags for the continuation).
+static int run_loop(epi_engine* h, uint32_t until = 0xFFFFFFFFu) {
     h->stop_rule = true;
-    int rc = run_loop_body(h);
+    int rc = run_loop_body(h, until);
     h->stop_rule = false;
+    if (rc) h->loop_hour = 0;  // a failed run cannot be continued
+    if (h->loop_hour != 0 && !rc) return EPI_OK;
     int rc2 = set_all_active(h);
     return rc ? rc : rc2;
 }
@@ -735,17 +742,21 @@ static int run_loop(epi_engine* h) {
 // waste while the host synchronises once per chain instead of once per day.
 constexpr uint32_t kChainHours = 24u * 8u;
 
-static int run_loop_body(epi_engine* h) {
+static int run_loop_body(epi_engine* h, uint32_t until) {
     uint32_t last = 0;  // last simulated hour over all replicates
-    for (auto& rep : h->reps) {
-        rep.rows.clear();
-        rep.active = rep.p.hours >= 2;
-        rep.hp.active = rep.active ? 1u : 0u;
-        if (rep.active) last = std::max(last, rep.p.hours - 1);
+    if (h->loop_hour == 0) {  // a fresh run
+        for (auto& rep : h->reps) {
+            rep.rows.clear();
+            rep.active = rep.p.hours >= 2;
+            rep.hp.active = rep.active ? 1u : 0u;
+        }
+        h->loop_hour = 1;
     }
-    uint32_t hour = 1;
+    for (const auto& rep : h->reps)
+        if (rep.p.hours >= 2) last = std::max(last, rep.p.hours - 1);
+    uint32_t hour = h->loop_hour;
     bool dirty = true;
-    while (hour <= last) {
+    while (hour <= last && hour <= until) {
         bool any = false;
         for (auto& rep : h->reps) any |= rep.active;
         if (!any) break;
@@ -757,7 +768,7 @@ static int run_loop_body(epi_engine* h) {
         // the chain ends at the first hour where the host must act whatever the counts are: a
         // replicate's final hour or fixed intervention; data-dependent triggers halt it on
         // the device at the day boundary where they fire
-        uint64_t end = std::min<uint64_t>(last, (uint64_t)hour + kChainHours - 1);
+        uint64_t end = std::min<uint64_t>(std::min(last, until), (uint64_t)hour + kChainHours - 1);
         for (const auto& rep : h->reps) {
             if (!rep.active) continue;
             end = std::min<uint64_t>(end, rep.p.hours - 1);
@@ -802,6 +813,9 @@ static int run_loop_body(epi_engine* h) {
         }
         hour = next;
     }
+    bool any = false;
+    for (const auto& rep : h->reps) any |= rep.active;
+    h->loop_hour = (any && hour <= last) ? hour : 0u;
     if (dirty) return push_params(h);
     return EPI_OK;
 }
@@ -1235,7 +1249,9 @@ static int save_state(epi_engine* h) {
         rep.s_geo = rep.geo;
         rep.s_hosp_code = rep.hp.hosp_code;
         rep.s_active = rep.active;
+        rep.s_rows = rep.rows;
     }
+    h->s_loop_hour = h->loop_hour;
     h->saved = true;
     return EPI_OK;
 }
@@ -1258,8 +1274,9 @@ static int restore_state(epi_engine* h) {
         rep.hp.hosp_code = rep.s_hosp_code;
         rep.active = rep.s_active;
         rep.hp.active = rep.s_active ? 1u : 0u;
-        rep.rows.clear();
+        rep.rows = rep.s_rows;
     }
+    h->loop_hour = h->s_loop_hour;
     return push_params(h);
 }
 
@@ -1488,6 +1505,182 @@ int epi_engine_run(epi_engine* h, epi_counts* rows, uint32_t max_rows, uint32_t*
         std::memcpy(rows, got.data(), nr * sizeof(epi_counts));
     }
     *n_rows = nr;
+    return EPI_OK;
+}
+
+int epi_engine_run_until(epi_engine* h, uint32_t last_hour, epi_counts* rows, uint32_t max_rows, uint32_t* n_rows,
+                         uint32_t* next_hour) {
+    if (!h || !n_rows || !next_hour) return EPI_ERR_ARG;
+    *n_rows = 0;
+    *next_hour = 0;
+    int rc = run_loop(h, last_hour);
+    if (rc) return rc;
+    const std::vector<epi_counts>& got = h->reps[0].rows;
+    const uint32_t nr = (uint32_t)got.size();
+    if (rows) {
+        if (max_rows < nr) { h->err = "rows buffer too small"; return EPI_ERR_ARG; }
+        std::memcpy(rows, got.data(), nr * sizeof(epi_counts));
+    }
+    *n_rows = nr;
+    *next_hour = h->loop_hour;
+    return EPI_OK;
+}
+
+}  // extern "C"
+
+// ---- checkpoint file
+namespace {
+constexpr uint32_t kCheckpointMagic = 0x4B435045u;  // "EPCK"
+constexpr uint32_t kCheckpointVersion = 1;
+
+uint64_t fnv1a64(const std::vector<uint8_t>& b) {  // FNV-1a (Fowler, Noll, Vo), 64-bit
+    uint64_t x = 0xCBF29CE484222325ull;
+    for (uint8_t c : b) {
+        x ^= c;
+        x *= 0x100000001B3ull;
+    }
+    return x;
+}
+template <typename T>
+void put(std::vector<uint8_t>& b, const T& v) {
+    const uint8_t* p = reinterpret_cast<const uint8_t*>(&v);
+    b.insert(b.end(), p, p + sizeof(T));
+}
+void put_bytes(std::vector<uint8_t>& b, const void* p, size_t n) {
+    b.insert(b.end(), static_cast<const uint8_t*>(p), static_cast<const uint8_t*>(p) + n);
+}
+void put_string(std::vector<uint8_t>& b, const std::string& s) {
+    put(b, (uint32_t)s.size());
+    put_bytes(b, s.data(), s.size());
+}
+struct Reader {
+    const std::vector<uint8_t>& b;
+    size_t at = 0;
+    bool ok = true;
+    bool bytes(void* dst, size_t n) {
+        if (!ok || n > b.size() - at) return ok = false;
+        std::memcpy(dst, b.data() + at, n);
+        at += n;
+        return true;
+    }
+    template <typename T>
+    bool get(T& v) { return bytes(&v, sizeof(T)); }
+    bool string(std::string& s) {
+        uint32_t n = 0;
+        if (!get(n) || n > b.size() - at) return ok = false;
+        s.assign(reinterpret_cast<const char*>(b.data() + at), n);
+        at += n;
+        return true;
+    }
+};
+}  // namespace
+
+extern "C" {
+
+int epi_engine_checkpoint_write(epi_engine* h, const char* path) {
+    if (!h || !path) return EPI_ERR_ARG;
+    if (h->R() != 1) { h->err = "checkpoints are for single engines"; return EPI_ERR_ARG; }
+    const Replica& rep = h->reps[0];
+    std::vector<epi_agent_record> recs(rep.n);
+    int rc = snapshot_replica(h, 0, recs.data(), recs.size());
+    if (rc) return rc;
+    std::vector<uint8_t> b;
+    for (uint32_t v : {kCheckpointMagic, kCheckpointVersion, (uint32_t)sizeof(epi_params), (uint32_t)sizeof(epi_geography),
+                       (uint32_t)sizeof(epi_agent_record), (uint32_t)sizeof(epi_counts), rep.n, h->loop_hour,
+                       (uint32_t)rep.rows.size(), (uint32_t)rep.iv.reports.size(), rep.active ? 1u : 0u,
+                       rep.iv.locked ? 1u : 0u, rep.iv.zero_infection_hour, rep.iv.new_infections_in_a_day,
+                       rep.iv.hospital_applied ? 1u : 0u})
+        put(b, v);
+    put(b, rep.p);
+    put(b, rep.geo);
+    put_bytes(b, rep.rows.data(), rep.rows.size() * sizeof(epi_counts));
+    for (const Report& r : rep.iv.reports) {
+        put(b, r.hour);
+        put_string(b, r.name);
+        put_string(b, r.data);
+    }
+    put_bytes(b, recs.data(), recs.size() * sizeof(epi_agent_record));
+    put(b, fnv1a64(b));
+    FILE* f = std::fopen(path, "wb");
+    if (!f) { h->err = std::string("checkpoint: cannot write ") + path; return EPI_ERR_IO; }
+    const bool ok = std::fwrite(b.data(), 1, b.size(), f) == b.size();
+    if (std::fclose(f) != 0 || !ok) { h->err = std::string("checkpoint: write failed: ") + path; return EPI_ERR_IO; }
+    return EPI_OK;
+}
+
+int epi_engine_create_from_checkpoint(const char* path, epi_engine** out) {
+    if (!path || !out) return EPI_ERR_ARG;
+    *out = nullptr;
+    auto fail = [](const std::string& m) {
+        g_create_error = "checkpoint: " + m;
+        return EPI_ERR_IO;
+    };
+    std::vector<uint8_t> b;
+    {
+        FILE* f = std::fopen(path, "rb");
+        if (!f) return fail(std::string("cannot read ") + path);
+        uint8_t buf[1 << 16];
+        size_t k;
+        while ((k = std::fread(buf, 1, sizeof buf, f)) > 0) b.insert(b.end(), buf, buf + k);
+        std::fclose(f);
+    }
+    if (b.size() < 15 * 4 + 8) return fail("truncated file");
+    uint64_t sum = 0;
+    std::memcpy(&sum, b.data() + b.size() - 8, 8);
+    b.resize(b.size() - 8);
+    if (fnv1a64(b) != sum) return fail("checksum mismatch (truncated or corrupt file)");
+    Reader rd{b};
+    uint32_t hdr[15];
+    for (uint32_t& v : hdr) rd.get(v);
+    if (hdr[0] != kCheckpointMagic) return fail("not a checkpoint file");
+    if (hdr[1] != kCheckpointVersion) return fail("unsupported version " + std::to_string(hdr[1]));
+    if (hdr[2] != sizeof(epi_params) || hdr[3] != sizeof(epi_geography) || hdr[4] != sizeof(epi_agent_record) ||
+        hdr[5] != sizeof(epi_counts))
+        return fail("written by a build with other struct layouts");
+    const uint32_t n = hdr[6], loop_hour = hdr[7], n_rows = hdr[8], n_reports = hdr[9];
+    epi_params p;
+    epi_geography geo;
+    rd.get(p);
+    rd.get(geo);
+    if (!rd.ok || p.number_of_agents != n || n == 0) return fail("inconsistent header");
+    if ((uint64_t)n_rows * sizeof(epi_counts) > b.size()) return fail("truncated file");
+    std::vector<epi_counts> rows(n_rows);
+    rd.bytes(rows.data(), rows.size() * sizeof(epi_counts));
+    std::vector<Report> reports(std::min<uint32_t>(n_reports, 1u << 20));
+    for (Report& r : reports) {
+        rd.get(r.hour);
+        rd.string(r.name);
+        rd.string(r.data);
+    }
+    if ((uint64_t)n * sizeof(epi_agent_record) > b.size()) return fail("truncated file");
+    std::vector<epi_agent_record> recs(n);
+    rd.bytes(recs.data(), recs.size() * sizeof(epi_agent_record));
+    if (!rd.ok || rd.at != b.size() || reports.size() != n_reports) return fail("truncated or malformed file");
+    const std::string bad = validate_params(p);
+    if (!bad.empty()) return fail(bad);
+    epi_engine* h = nullptr;
+    const epi_agent_record* one[1] = {recs.data()};
+    int rc = create_engine(&p, one, 1, &h);
+    if (rc) return rc;
+    Replica& rep = h->reps[0];
+    rep.geo = geo;
+    rep.hp.hosp_code = rect_eq(to_rect(geo.hospital), rep.hp.area[kHosp0]) ? kHosp0 : kHosp1;
+    rep.iv.locked = hdr[11] != 0;
+    rep.iv.zero_infection_hour = hdr[12];
+    rep.iv.new_infections_in_a_day = hdr[13];
+    rep.iv.hospital_applied = hdr[14] != 0;
+    rep.iv.reports = std::move(reports);
+    rep.rows = std::move(rows);
+    rep.active = hdr[10] != 0;
+    rep.hp.active = rep.active ? 1u : 0u;
+    h->loop_hour = loop_hour;
+    rc = push_params(h);
+    if (rc) {
+        g_create_error = h->err;
+        epi_engine_destroy(h);
+        return rc;
+    }
+    *out = h;
     return EPI_OK;
 }
 

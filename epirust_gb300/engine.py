@@ -104,6 +104,20 @@ def world_build(params: EpiParams) -> tuple[np.ndarray, EpiGeography]:
     return recs, g
 
 
+CHECKPOINT_HEADER_WORDS = 15  # u32 words before the parameters (epi_engine_checkpoint_write)
+
+
+def checkpoint_params(path: str) -> EpiParams:
+    """The parameters stored in a checkpoint file (they follow its 15-word header)."""
+    with open(path, "rb") as f:
+        head = f.read(4 * CHECKPOINT_HEADER_WORDS + C.sizeof(EpiParams))
+    words = np.frombuffer(head[: 4 * CHECKPOINT_HEADER_WORDS], dtype="<u4")
+    if len(head) < 4 * CHECKPOINT_HEADER_WORDS + C.sizeof(EpiParams) or words[0] != 0x4B435045 \
+            or words[2] != C.sizeof(EpiParams):
+        raise ValueError(f"{path}: not a checkpoint of this build")
+    return EpiParams.from_buffer_copy(head[4 * CHECKPOINT_HEADER_WORDS:])
+
+
 class Epidemiology:
     """One single-region engine on the GPU."""
 
@@ -181,12 +195,38 @@ class Epidemiology:
 
     # -- the run loop
     def run(self) -> np.ndarray:
-        """run_single_engine: hours 1..hours-1 with interventions and the stop rule."""
+        """run_single_engine: hours 1..hours-1 with interventions and the stop rule (a run
+        paused by run_until continues where it stopped; the rows start at hour 1)."""
         cap = max(self.params.hours, 1)
         rows = np.zeros(cap, dtype=COUNTS_DTYPE)
         n = C.c_uint32(0)
         check(lib().epi_engine_run(self._h, rows.ctypes.data, cap, C.byref(n)), self._h)
         return rows[: n.value]
+
+    def run_until(self, last_hour: int) -> tuple[np.ndarray, int]:
+        """The run loop paused after last_hour: (rows so far, the hour it continues from, 0 when
+        the run has ended)."""
+        cap = max(self.params.hours, 1)
+        rows = np.zeros(cap, dtype=COUNTS_DTYPE)
+        n, nxt = C.c_uint32(0), C.c_uint32(0)
+        check(lib().epi_engine_run_until(self._h, last_hour, rows.ctypes.data, cap, C.byref(n), C.byref(nxt)), self._h)
+        return rows[: n.value], nxt.value
+
+    def save_checkpoint(self, path: str) -> None:
+        """Write the world, its intervention state and a paused run's position to a file."""
+        check(lib().epi_engine_checkpoint_write(self._h, str(path).encode()), self._h)
+
+    @classmethod
+    def from_checkpoint(cls, path: str) -> "Epidemiology":
+        """An engine resumed from save_checkpoint's file (run() continues a paused run)."""
+        h = C.c_void_p()
+        check(lib().epi_engine_create_from_checkpoint(str(path).encode(), C.byref(h)), None)
+        self = cls.__new__(cls)
+        self._h = h
+        self.config = None
+        self.rows = []
+        self.params = checkpoint_params(str(path))
+        return self
 
     def write_outputs(self, output_dir: str, engine_id: str = "0") -> None:
         check(lib().epi_engine_write_outputs(self._h, output_dir.encode(), engine_id.encode()), self._h)

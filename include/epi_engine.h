@@ -30,7 +30,7 @@ enum {
     EPI_ERR_TIMEOUT = 4,   /* a bounded device-side wait gave up                          */
     EPI_ERR_INVARIANT = 5, /* a consistency check failed (counts total != population)    */
     EPI_ERR_ARG = 6,       /* bad argument (null pointer, short buffer, hour out of range) */
-    EPI_ERR_IO = 7         /* output file could not be written                            */
+    EPI_ERR_IO = 7         /* a file could not be written, read or was not what it claims   */
 };
 
 /* ---------------------------------------------------------------- enumerations */
@@ -235,8 +235,24 @@ int epi_engine_increase_hospital_size(epi_engine* h);           /* grid.rs:233-2
 
 /* Epidemiology::run_single_engine (engine/src/epidemiology_simulation.rs:211-274):
  * hours 1 .. hours-1 with interventions and the standalone stop rule.  rows gets one
- * epi_counts per simulated hour (capacity max_rows >= hours-1); *n_rows the number written. */
+ * epi_counts per simulated hour (capacity max_rows >= hours-1); *n_rows the number written.
+ * A run paused by epi_engine_run_until continues where it stopped (rows from hour 1). */
 int epi_engine_run(epi_engine* h, epi_counts* rows, uint32_t max_rows, uint32_t* n_rows);
+
+/* The same run loop, paused after hour last_hour (no reference counterpart): rows so far as
+ * epi_engine_run gives them; *next_hour is the hour the run continues from, or 0 when it has
+ * ended.  Direct hour calls (epi_engine_simulate*) do not advance a paused run. */
+int epi_engine_run_until(epi_engine* h, uint32_t last_hour, epi_counts* rows, uint32_t max_rows, uint32_t* n_rows,
+                         uint32_t* next_hour);
+
+/* On-disk checkpoint of a single engine (no reference counterpart): the parameters, the
+ * current geography, every agent record, the intervention state and reports, the rows and
+ * the position of a paused run.  With counter-based random streams the resumed run is the
+ * uninterrupted one, bit for bit.  File: "EPCK", version, struct sizes, then the parts in
+ * that order and an FNV-1a 64 checksum of everything before it.  A file that is missing,
+ * truncated, of another version or whose checksum differs gives EPI_ERR_IO. */
+int epi_engine_checkpoint_write(epi_engine* h, const char* path);
+int epi_engine_create_from_checkpoint(const char* path, epi_engine** out);
 
 /* Listeners: CsvListener + InterventionReporter (engine/src/listeners/csv_service.rs:61-71,
  * intervention_reporter.rs:52-63).  Writes <dir>/output/simulation_<engine_id>_<UTC time>.csv
@@ -257,10 +273,10 @@ int epi_engine_geography(const epi_engine* h, epi_geography* out);
  * exactly population occupied cells. */
 int epi_engine_check(epi_engine* h);
 
-/* Device-side checkpoint of the agent state, the plane, the intervention state and the
- * hospital (the reference has none; its counts live only in memory until the end,
- * engine/src/listeners/csv_service.rs:61-71).  restore_state rewinds to the last save;
- * with counter-based random streams a rewound run repeats itself exactly. */
+/* Device-side checkpoint of the agent state, the plane, the intervention state, the
+ * hospital and the position of a paused run (the reference has none; its counts live only in
+ * memory until the end, engine/src/listeners/csv_service.rs:61-71).  restore_state rewinds
+ * to the last save; with counter-based random streams a rewound run repeats itself exactly. */
 int epi_engine_save_state(epi_engine* h);
 int epi_engine_restore_state(epi_engine* h);
 
