@@ -840,14 +840,16 @@ static void free_device(epi_engine* h) {
 static size_t align_up(size_t v, size_t a) { return (v + a - 1) / a * a; }
 
 // Pack one replicate's records into the host mirrors of the SoA arrays.
+// Records i0 .. i1 - 1 of replicate r.
 static int pack_replica(const epi_engine* h, uint32_t r, const epi_agent_record* recs, uint32_t* pos, uint2* st,
-                        uint32_t* home, uint32_t* work, uint32_t* wsa, std::string& err) {
+                        uint32_t* home, uint32_t* work, uint32_t* wsa, std::string& err, uint32_t i0 = 0,
+                        uint32_t i1 = 0xFFFFFFFFu) {
     const Replica& rep = h->reps[r];
     const int32_t G = (int32_t)rep.p.grid_size;
     auto inside = [G](int32_t x0, int32_t y0, int32_t x1, int32_t y1) {
         return x0 >= 0 && y0 >= 0 && x1 <= G && y1 <= G && x0 <= x1 && y0 <= y1;
     };
-    for (uint32_t i = 0; i < rep.n; ++i) {
+    for (uint32_t i = i0; i < std::min(i1, rep.n); ++i) {
         const epi_agent_record& a = recs[i];
         if (a.x < 0 || a.y < 0 || a.x > G || a.y > G || a.state > EPI_D || a.work_status > EPI_WS_NA ||
             a.immunity < -2 || a.immunity > 2 || a.infection_day > 0xFFFFu ||
@@ -1047,21 +1049,29 @@ static int engine_init(epi_engine* h, const epi_params* params, const epi_agent_
         if (rc) return rc;
         return finish_upload(h);
     }
-    // host mirrors, filled per replicate (in parallel for large ensembles)
+    // host mirrors, filled in parallel: pieces of at most 64K records of any replicate
     std::vector<uint32_t> pos(slots, 0), home(slots, 0), work(slots, 0), wsa(slots, 0);
     std::vector<uint2> st(slots, make_uint2(0, 0));
-    std::vector<int> status(R, EPI_OK);
-    std::vector<std::string> errs(R);
-    const unsigned workers = std::max(1u, std::min<unsigned>(R, std::thread::hardware_concurrency()));
+    constexpr uint32_t kPackPiece = 1u << 16;
+    std::vector<std::pair<uint32_t, uint32_t>> pieces;  // (replicate, first record)
+    for (uint32_t r = 0; r < R; ++r)
+        for (uint32_t i = 0; i < h->reps[r].n; i += kPackPiece) pieces.emplace_back(r, i);
+    std::vector<int> status(pieces.size(), EPI_OK);
+    std::vector<std::string> errs(pieces.size());
+    const unsigned workers =
+        std::max(1u, std::min<unsigned>((unsigned)pieces.size(), std::thread::hardware_concurrency()));
     std::vector<std::thread> pool;
     for (unsigned w = 0; w < workers; ++w)
         pool.emplace_back([&, w] {
-            for (uint32_t r = w; r < R; r += workers)
-                status[r] = pack_replica(h, r, recs[r], pos.data(), st.data(), home.data(), work.data(), wsa.data(), errs[r]);
+            for (size_t k = w; k < pieces.size(); k += workers) {
+                const uint32_t r = pieces[k].first, i0 = pieces[k].second;
+                status[k] = pack_replica(h, r, recs[r], pos.data(), st.data(), home.data(), work.data(), wsa.data(),
+                                         errs[k], i0, i0 + kPackPiece);
+            }
         });
     for (auto& t : pool) t.join();
-    for (uint32_t r = 0; r < R; ++r)
-        if (status[r]) { h->err = errs[r]; return status[r]; }
+    for (size_t k = 0; k < pieces.size(); ++k)  // the first bad record in (replicate, index) order
+        if (status[k]) { h->err = errs[k]; return status[k]; }
     CK(cudaMemcpyAsync(h->d_pos, pos.data(), slots * sizeof(uint32_t), cudaMemcpyHostToDevice, h->stream));
     CK(cudaMemcpyAsync(h->d_home, home.data(), slots * sizeof(uint32_t), cudaMemcpyHostToDevice, h->stream));
     CK(cudaMemcpyAsync(h->d_work, work.data(), slots * sizeof(uint32_t), cudaMemcpyHostToDevice, h->stream));
