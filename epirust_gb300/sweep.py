@@ -149,6 +149,9 @@ def screened_sweep(net, candidates: int = 65_536, keep: int = 256, replicates: i
         "random_best_curve_mse": float(err_r[pick_r]),
         "random_best_peak_rel_err_vs_target": float(relative_peak_error(mean_r[pick_r:pick_r + 1], target[None],
                                                                          days)[0]),
+        # candidates whose ABM replicate-mean peak lies within 5 % of the target's, by stage
+        "screened_within_5pct_of_target_peak": int((relative_peak_error(mean_s, target[None], days) <= 0.05).sum()),
+        "random_within_5pct_of_target_peak": int((relative_peak_error(mean_r, target[None], days) <= 0.05).sum()),
         "abm_only_sweep_s_estimated": abm_only_s, "screened_sweep_s": screened_s,
         "sweep_speedup": abm_only_s / screened_s,
     }
