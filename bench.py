@@ -237,8 +237,28 @@ def run_batched(args, stream, flush) -> dict:
         ev1.synchronize()
         ms_total += ev0.elapsed_time(ev1)
         agent_hours += sum(float(p.number_of_agents) * len(r) for p, r in zip(params, rows))
+    # roofline of the ensemble's dominant kernel: one more run with event nodes around every kernel
+    ens.restore_state()
+    ens.set_profiling(True)
+    ens.run()
+    stats = ens.kernel_stats()
     ens.close()
     batched_value = agent_hours / (ms_total / 1000.0)
+    launches_d, ms_d = stats["k_decide"]
+    avg_ms = ms_d / max(launches_d, 1)
+    cells = sum((p.grid_size + 1) ** 2 for p in params)
+    alg = DECIDE_BYTES_PER_AGENT * agents + DECIDE_PLANES * cells
+    peak, peak_kind = _peaks()
+    traffic = None
+    tpath = os.path.join(ROOT, "profiles", "k_decide_ens_traffic.txt")
+    if os.path.exists(tpath):
+        with open(tpath) as f:
+            captured = int(f.readline().rsplit(":", 1)[1])
+        traffic = int(captured * agents / 30_602_061)  # captured on this workload; scales with agents
+    roofline = {"bound": "hbm", "kernel": "k_decide_ens", "achieved": alg / (avg_ms / 1000.0) / 1e9, "peak": peak,
+                "unit": "GB/s", "frac": alg / (avg_ms / 1000.0) / 1e9 / peak, "peak_kind": peak_kind,
+                "traffic": traffic, "alg_bytes_per_launch": alg, "avg_launch_ms": avg_ms,
+                "kernels": {k: {"launches": v[0], "ms": v[1]} for k, v in stats.items() if v[0]}}
 
     # the same replicates one at a time through the plain single-engine path (every 4th one,
     # graphs warm: one untimed run per engine first)
@@ -265,7 +285,7 @@ def run_batched(args, stream, flush) -> dict:
             "sequential_plain_value": sequential_value, "sequential_sample": len(sample),
             "speedup_vs_sequential_plain": batched_value / sequential_value,
             "ms_per_step": ms_total / steps, "steps": steps, "world_build_and_upload_s": build_s,
-            "launch_shape": shape,
+            "launch_shape": shape, "roofline": roofline,
             "workload": "256 replicates, populations log-uniform in [10k, 500k], grid ceil(sqrt(N/0.16)), regular "
                         "rate U[0.02, 0.10], 0.05% exposed, 2400 h, no interventions, seeds from 11"}
 

@@ -4,6 +4,9 @@ package and exits.
     python -m epirust_gb300.profile_cases tick --agents 1000000 --grid 2500 --hours 48
         the config-2 world (tests/golden/c2_small_pox_1m.json) resized, hours 1..hours-1
         through simulate_hours (one CUDA graph per call); --events adds CUDA events per kernel
+    python -m epirust_gb300.profile_cases ensemble --replicates 256 --hours 49
+        the config-3 ensemble (256 replicates, 30.6M agents) through the run loop, hours
+        1..hours-1
     python -m epirust_gb300.profile_cases mlp-train --steps 30 [--members M]
         the surrogate network 8 -> 512 x 3 -> 600 (M members in one handle), batch 256, on a
         seeded synthetic set of 4,096 samples: `steps` Adam steps (one graph replay each)
@@ -40,6 +43,24 @@ def tick(args) -> dict:
         out["kernels"] = {k: v for k, v in eng.kernel_stats().items() if v[0]}
     eng.close()
     return out
+
+
+def ensemble(args) -> dict:
+    """The config-3 ensemble (256 replicates, 10k-500k agents) through the run loop for
+    hours 1..hours-1."""
+    from .engine import Ensemble
+    from .workloads import ensemble_params
+
+    params = ensemble_params(replicates=args.replicates)
+    for p in params:
+        p.hours = args.hours
+    ens = Ensemble(params)
+    t0 = time.perf_counter()
+    rows = ens.run()
+    dt = time.perf_counter() - t0
+    ah = sum(float(p.number_of_agents) * len(r) for p, r in zip(params, rows))
+    ens.close()
+    return {"replicates": len(params), "hours": args.hours - 1, "s": dt, "agent_hours_per_s": ah / dt}
 
 
 def _net(members: int = 1):
@@ -83,6 +104,9 @@ def main() -> None:
     t.add_argument("--grid", type=int, default=2500)
     t.add_argument("--hours", type=int, default=48)
     t.add_argument("--events", action="store_true")
+    e = sub.add_parser("ensemble")
+    e.add_argument("--replicates", type=int, default=256)
+    e.add_argument("--hours", type=int, default=49)
     m = sub.add_parser("mlp-train")
     m.add_argument("--steps", type=int, default=30)
     m.add_argument("--members", type=int, default=1)
@@ -90,7 +114,7 @@ def main() -> None:
     s.add_argument("--candidates", type=int, default=65536)
     s.add_argument("--members", type=int, default=1)
     args = ap.parse_args()
-    fn = {"tick": tick, "mlp-train": mlp_train, "mlp-screen": mlp_screen}[args.case]
+    fn = {"tick": tick, "ensemble": ensemble, "mlp-train": mlp_train, "mlp-screen": mlp_screen}[args.case]
     print(json.dumps(fn(args)))
 
 

@@ -122,3 +122,23 @@ def test_save_restore_keeps_the_run_position(gpu):
     rows, nxt = eng.run_until(10)
     assert len(rows) == 10 and nxt == 11
     eng.close()
+
+
+@pytest.mark.gpu
+def test_pauses_at_event_hours(gpu):
+    """Pauses at the first hour, at day boundaries, around the vaccination hour and at the
+    last hour all resume to the uninterrupted run."""
+    ref = _engine()
+    want = ref.run()
+    ref.close()
+    eng = _engine()
+    for pause in (1, 24, 199, 200, 201, 479, len(want) - 1):
+        eng.save_state()
+        rows, nxt = eng.run_until(pause)
+        assert _same(rows, want[:pause]) and nxt == pause + 1, pause
+        got = eng.run()
+        assert _same(got, want), pause
+        eng.restore_state()
+    rows, nxt = eng.run_until(10**6)
+    assert _same(rows, want) and nxt == 0
+    eng.close()
