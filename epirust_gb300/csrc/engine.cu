@@ -347,20 +347,23 @@ static int commit_blocks_for(uint32_t slots, int per_thread = kCommitSlots) {
     return (int)std::max<uint32_t>(1u, (slots + per_block - 1) / per_block);
 }
 
-// k_commit with S slots per thread and round.
+// k_commit with S slots per thread and round; the sparse instance for the hours of day 0 and
+// 23, where hardly any agent acts.
 using CommitKernel = void (*)(const DevParams*, const uint32_t*, uint32_t, uint32_t*, const uint32_t*, uint8_t*,
                               uint8_t*, uint32_t*, const uint32_t*, HourArgs, uint64_t);
-static CommitKernel commit_kernel(int slots_per_thread) {
+static CommitKernel commit_kernel(int slots_per_thread, bool sparse = false) {
+#define EPI_PICK(S) (sparse ? (CommitKernel)k_commit<S, true> : (CommitKernel)k_commit<S, false>)
     switch (slots_per_thread) {
-        case 1: return k_commit<1>;
-        case 2: return k_commit<2>;
-        case 3: return k_commit<3>;
-        case 4: return k_commit<4>;
-        case 5: return k_commit<5>;
-        case 6: return k_commit<6>;
-        case 7: return k_commit<7>;
-        default: return k_commit<8>;
+        case 1: return EPI_PICK(1);
+        case 2: return EPI_PICK(2);
+        case 3: return EPI_PICK(3);
+        case 4: return EPI_PICK(4);
+        case 5: return EPI_PICK(5);
+        case 6: return EPI_PICK(6);
+        case 7: return EPI_PICK(7);
+        default: return EPI_PICK(8);
     }
+#undef EPI_PICK
 }
 
 // k_commit grid for S slots per thread: every slot once.  (Capping it at one wave of
@@ -405,7 +408,7 @@ static int enqueue_piece(epi_engine* h, uint32_t first_hour, uint32_t nh) {
                                   (const uint32_t*)h->d_home, (const uint32_t*)h->d_work, h->d_wsa,
                                   (const uint8_t*)h->d_plane, (const uint8_t*)h->d_danger, h->d_claim, h->d_tgt, h->d_lost,
                                   ha, h->d_err)));
-            const CommitKernel commit = commit_kernel(h->commit_slots);
+            const CommitKernel commit = commit_kernel(h->commit_slots, hod == 0u || hod == 23u);
             LAUNCH(kKCommit, CK(launch_hour_kernel(commit, h->commit_blocks, h->stream, (const DevParams*)h->d_params,
                                                    (const uint32_t*)h->d_chunk_rep, h->slots, h->d_pos,
                                                    (const uint32_t*)h->d_tgt, h->d_plane, h->d_danger, h->d_claim,
