@@ -3,7 +3,8 @@ package and exits.
 
     python -m epirust_gb300.profile_cases tick --agents 1000000 --grid 2500 --hours 48
         the config-2 world (tests/golden/c2_small_pox_1m.json) resized, hours 1..hours-1
-        through simulate_hours (one CUDA graph per call); --events adds CUDA events per kernel
+        through simulate_hours (one CUDA graph per call); --events adds CUDA events per kernel,
+        --shape 608,2 sets the launch shape (k_decide grid, agents per k_commit thread)
     python -m epirust_gb300.profile_cases ensemble --replicates 256 --hours 49
         the config-3 ensemble (256 replicates, 30.6M agents) through the run loop, hours
         1..hours-1
@@ -34,6 +35,8 @@ def tick(args) -> dict:
     cfg["population"]["Auto"]["number_of_agents"] = args.agents
     cfg["geography_parameters"]["grid_size"] = args.grid
     eng = Epidemiology(Config(json.dumps(cfg)))
+    if args.shape:  # "blocks,slots": the k_decide grid and agents per k_commit thread
+        eng.set_launch_shape(*(int(v) for v in args.shape.split(",")))
     eng.set_profiling(args.events)
     t0 = time.perf_counter()
     eng.simulate_hours(1, args.hours - 1)
@@ -104,6 +107,7 @@ def main() -> None:
     t.add_argument("--grid", type=int, default=2500)
     t.add_argument("--hours", type=int, default=48)
     t.add_argument("--events", action="store_true")
+    t.add_argument("--shape", default="", help="launch shape 'blocks,slots' (k_decide grid, agents per k_commit thread)")
     e = sub.add_parser("ensemble")
     e.add_argument("--replicates", type=int, default=256)
     e.add_argument("--hours", type=int, default=49)
