@@ -138,6 +138,15 @@ struct Draws {
         if (!(have & 8u)) { philox2x32(agent | kMoveChoice, hour, mk, ch); have |= 8u; }
         return ch[0];
     }
+    // One movement block chosen per lane (the point block when go, else the choice block),
+    // computed before a work-status branch so that a warp whose lanes take both arms runs
+    // the Philox rounds once instead of once per arm; the words are the ones m() returns.
+    __device__ __forceinline__ void prime(bool go) {
+        uint32_t o[2];
+        philox2x32(agent | (go ? kMovePoint : kMoveChoice), hour, mk, o);
+        if (go) { pt[0] = o[0]; pt[1] = o[1]; have |= 1u; }
+        else { ch[0] = o[0]; ch[1] = o[1]; have |= 8u; }
+    }
     __device__ __forceinline__ uint32_t d(int w) {
         if (!(have & 2u)) { philox4x32(agent, hour, kBlkDisease, 0u, k0, k1, b1); have |= 2u; }
         return b1[w];
@@ -332,6 +341,8 @@ __device__ __forceinline__ Cell perform_movements(const DevParams& P, const Plan
     } else {
         const Rect cur = area_rect(P, st_area(s), home, work);
         const bool worker = ws != EPI_WS_NA;  // Normal or Essential here
+        if (HC != kHcMove)  // the arm below that goes to an area draws a random point, the other walks
+            dr.prime(HC == kHcTransport ? worker && (s & kPt) : HC == kHcWork ? true : HC == kHcNoon ? !worker : worker);
         if (HC == kHcMove) {
             nc = move_agent_from(pl, s, cur, cell, dr);
         } else if (HC == kHcTransport) {
