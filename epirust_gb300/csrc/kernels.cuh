@@ -376,7 +376,7 @@ __global__ void __launch_bounds__(kThreads) k_commit(const DevParams* __restrict
                 rplane[old_cell] = 0;
                 rplane[new_cell] = (uint8_t)cls;
                 pos[slot] = xy;
-            } else {
+            } else if (cls != cls0) {  // a beaten mover whose class held keeps its byte as it is
                 rplane[old_cell] = (uint8_t)cls;
             }
             // infectious-neighbour counts follow infectious agents that move or stop or start
