@@ -1939,7 +1939,7 @@ constexpr size_t kNoAllocErrOff = 264;                      // int error flags
 constexpr size_t kNoAllocTgtOff = 512;                      // u32 per agent
 static_assert(sizeof(DevParams) <= kNoAllocHourOff, "parameter block must fit its slot");
 
-__device__ __align__(256) unsigned char g_noalloc_scratch[kNoAllocScratchBytes];
+static __device__ __align__(256) unsigned char g_noalloc_scratch[kNoAllocScratchBytes];
 
 struct NoAllocDevice {
     unsigned char* base = nullptr;  // device address of g_noalloc_scratch on this device
