@@ -5,6 +5,8 @@ package and exits.
         the config-2 world (tests/golden/c2_small_pox_1m.json) resized, hours 1..hours-1
         through simulate_hours (one CUDA graph per call); --events adds CUDA events per kernel,
         --shape 608,2 sets the launch shape (k_decide grid, agents per k_commit thread)
+    python -m epirust_gb300.profile_cases run [--shape 608,2]
+        the config-2 run loop once (bench.py's step: 4,799 hours with the interventions)
     python -m epirust_gb300.profile_cases ensemble --replicates 256 --hours 49
         the config-3 ensemble (256 replicates, 30.6M agents) through the run loop, hours
         1..hours-1
@@ -46,6 +48,24 @@ def tick(args) -> dict:
         out["kernels"] = {k: v for k, v in eng.kernel_stats().items() if v[0]}
     eng.close()
     return out
+
+
+def run(args) -> dict:
+    """The config-2 run loop (1M agents, 2,500 grid, 4,800 h, lockdown, vaccination and the
+    hospital build): the workload of bench.py's step, once, at the launch shape given."""
+    from .engine import Config, Epidemiology
+
+    with open(C2) as f:
+        cfg = json.load(f)
+    eng = Epidemiology(Config(json.dumps(cfg)))
+    if args.shape:
+        eng.set_launch_shape(*(int(v) for v in args.shape.split(",")))
+    t0 = time.perf_counter()
+    rows = eng.run()
+    dt = time.perf_counter() - t0
+    n = cfg["population"]["Auto"]["number_of_agents"]
+    eng.close()
+    return {"hours": len(rows), "s": dt, "agent_hours_per_s": n * len(rows) / dt}
 
 
 def ensemble(args) -> dict:
@@ -108,6 +128,8 @@ def main() -> None:
     t.add_argument("--hours", type=int, default=48)
     t.add_argument("--events", action="store_true")
     t.add_argument("--shape", default="", help="launch shape 'blocks,slots' (k_decide grid, agents per k_commit thread)")
+    r = sub.add_parser("run")
+    r.add_argument("--shape", default="608,2", help="launch shape 'blocks,slots' (k_decide grid, agents per k_commit thread)")
     e = sub.add_parser("ensemble")
     e.add_argument("--replicates", type=int, default=256)
     e.add_argument("--hours", type=int, default=49)
@@ -118,7 +140,7 @@ def main() -> None:
     s.add_argument("--candidates", type=int, default=65536)
     s.add_argument("--members", type=int, default=1)
     args = ap.parse_args()
-    fn = {"tick": tick, "ensemble": ensemble, "mlp-train": mlp_train, "mlp-screen": mlp_screen}[args.case]
+    fn = {"tick": tick, "run": run, "ensemble": ensemble, "mlp-train": mlp_train, "mlp-screen": mlp_screen}[args.case]
     print(json.dumps(fn(args)))
 
 
