@@ -334,7 +334,7 @@ def run_gpu(args, cfg):
 
     eng = Epidemiology(config, records=records)
     eng.set_stream(stream.cuda_stream)
-    shape = eng.autotune(24)  # launch shapes of the tick kernels (results do not depend on them)
+    shape = eng.autotune(72)  # launch shapes of the tick kernels (results do not depend on them)
     eng.save_state()
 
     def step():

@@ -1215,7 +1215,7 @@ static int autotune(epi_engine* h, uint32_t hours, epi_launch_shape* out) {
         for (uint32_t c : slot_cands) {
             rc = set_launch_shape(h, g, c);
             double t_min = 1e300;
-            for (int rep = 0; rep < 3 && !rc; ++rep) {  // the first pass captures the graphs
+            for (int rep = 0; rep < 5 && !rc; ++rep) {  // the first pass captures the graphs
                 rc = restore_state(h);
                 if (rc) break;
                 const auto t0 = std::chrono::steady_clock::now();
