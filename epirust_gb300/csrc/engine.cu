@@ -1198,7 +1198,10 @@ static int autotune(epi_engine* h, uint32_t hours, epi_launch_shape* out) {
     if (hours == 0 || hours > 24u * 7u) { h->err = "autotune hours must be in [1, 168]"; return EPI_ERR_ARG; }
     const uint32_t n_chunks = h->slots / kChunk;
     std::vector<uint32_t> grids;
-    const uint64_t cand[3] = {(uint64_t)h->resident_blocks, 2ull * (uint64_t)h->resident_blocks, (uint64_t)n_chunks};
+    // three quarters of the resident grid too: fewer warps per SM share the L1 that holds the
+    // plane rows their agents read
+    const uint64_t cand[4] = {(uint64_t)h->resident_blocks * 3u / 4u, (uint64_t)h->resident_blocks,
+                              2ull * (uint64_t)h->resident_blocks, (uint64_t)n_chunks};
     for (uint64_t g : cand) {
         const uint32_t v = (uint32_t)std::max<uint64_t>(1, std::min<uint64_t>(g, n_chunks));
         if (std::find(grids.begin(), grids.end(), v) == grids.end()) grids.push_back(v);

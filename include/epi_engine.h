@@ -303,9 +303,9 @@ int epi_engine_state_stream_open(epi_engine* h, const char* path);
 int epi_engine_state_stream_close(epi_engine* h);
 
 /* Autotuner (no reference counterpart): time hours 1..hours (<= 168) of the current world
- * under each candidate shape -- k_decide grid = resident blocks, twice that, or one chunk per
- * block; 1, 2 or 4 agents per k_commit thread -- from the same starting state, keep the
- * fastest and restore the state.  Call it before simulating; it replaces the checkpoint of
+ * under each candidate shape -- k_decide grid = three quarters of the resident blocks, the
+ * resident blocks, twice that, or one chunk per block; 1, 2 or 4 agents per k_commit thread --
+ * from the same starting state, keep the fastest and restore the state.  Call it before simulating; it replaces the checkpoint of
  * epi_engine_save_state. */
 int epi_engine_autotune(epi_engine* h, uint32_t hours, epi_launch_shape* chosen);
 int epi_engine_set_launch_shape(epi_engine* h, const epi_launch_shape* shape);
