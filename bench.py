@@ -2,7 +2,7 @@
 
 Workload: the 1,000,000-agent / 2,500-grid run of 4,800 hours (small pox; 50 exposed;
 Lockdown at 1,000 infections with 10% essential workers; vaccination of 20% of the
-susceptible at hour 2,400; hospital build at 70% occupancy) -- tests/golden/c2_small_pox_1m.json.
+susceptible at hour 2,400; hospital build at 70% occupancy) -- tests/golden/small_pox_1m_2500.json.
 
 One step = one full run of that workload (epi_engine_run: all hours, interventions and the
 stop rule), restarted from the same initial world (a device-side restore) each step.
@@ -31,7 +31,7 @@ import time
 ROOT = os.path.dirname(os.path.abspath(__file__))
 sys.path.insert(0, ROOT)
 
-DEFAULT_CONFIG = os.path.join(ROOT, "tests", "golden", "c2_small_pox_1m.json")
+DEFAULT_CONFIG = os.path.join(ROOT, "tests", "golden", "small_pox_1m_2500.json")
 METRIC = "agent-hours/s"
 # Algorithmic bytes of one k_decide launch per agent: pos 4 + st 8 + home 4 + work 4 read,
 # st 8 + tgt 4 written; plus one read of the (G+1)^2 byte occupancy plane and of the
@@ -207,7 +207,7 @@ def run_reference(args, cfg):
 
 
 def run_batched(args, stream, flush) -> dict:
-    """Config 3: 256 replicates (10k-500k agents, sqrt grids, 2,400 h) in one launch per hour."""
+    """The batched ensemble: 256 replicates (10k-500k agents, sqrt grids, 2,400 h) in one launch per hour."""
     import torch
 
     from epirust_gb300 import Ensemble
@@ -449,7 +449,7 @@ def run_gpu(args, cfg):
             "warmup": args.warmup, "ms_per_step": ms_total / args.steps, "higher_is_better": True,
             "scaling": "weak", "vs_baseline": None, "dtype": "u32", "data": "synthetic",
             "config": {"workload": "plain single-engine tick: 1M agents, 2500 grid, 4800 h, lockdown + "
-                                   "vaccination + hospital build (tests/golden/c2_small_pox_1m.json)",
+                                   "vaccination + hospital build (tests/golden/small_pox_1m_2500.json)",
                        "agents": n, "grid": G, "hours_per_step": hours_per_step, "parallelism": f"replicas{world}",
                        "l2": "flushed between steps (512 MiB write); inputs L2-resident within a step",
                        "launch_shape": shape, "wall_s": wall},

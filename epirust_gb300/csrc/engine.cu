@@ -483,7 +483,7 @@ static int check_error_flag(epi_engine* h);
 
 // Longest piece (one captured graph): two days.  Back-to-back pieces cost nothing measurable
 // on the device, while every new engine captures its pieces once: two-day pieces made a
-// fresh engine's config-2 run 1.5 % faster than eight-day ones, at equal speed once warm.
+// fresh engine's 1M-agent 4,800-hour run 1.5 % faster than eight-day ones, at equal speed once warm.
 constexpr uint32_t kPieceHours = 24u * 2u;
 
 // Simulate hours first_hour .. first_hour + nh - 1 for every active replicate as one chain:

@@ -47,7 +47,7 @@ __device__ __forceinline__ void count_into(uint32_t* sh, bool valid, uint32_t bi
 
 // Consecutive chunks a block takes per grid-stride step.  An ensemble block that strides one
 // chunk at a time switches replicate at nearly every step (a parameter reload and a
-// histogram flush); groups of 8 made config 3 (256 replicates) 10 % faster.  A single world
+// histogram flush); groups of 8 made the 256-replicate ensemble 10 % faster.  A single world
 // keeps 1: the plain stride, where the resident blocks sweep one contiguous band of agents,
 // was measured fastest (groups of 2, 4, 8 were 2, 8, 15 % slower, a scattered chunk order
 // 6 % slower).

@@ -2,13 +2,13 @@
 package and exits.
 
     python -m epirust_gb300.profile_cases tick --agents 1000000 --grid 2500 --hours 48
-        the config-2 world (tests/golden/c2_small_pox_1m.json) resized, hours 1..hours-1
+        the 1M-agent / 2,500-grid small-pox world (tests/golden/small_pox_1m_2500.json) resized, hours 1..hours-1
         through simulate_hours (one CUDA graph per call); --events adds CUDA events per kernel,
         --shape 608,2 sets the launch shape (k_decide grid, agents per k_commit thread)
     python -m epirust_gb300.profile_cases run [--shape 608,2]
-        the config-2 run loop once (bench.py's step: 4,799 hours with the interventions)
+        the 1M-agent / 2,500-grid run loop once (bench.py's step: 4,799 hours with the interventions)
     python -m epirust_gb300.profile_cases ensemble --replicates 256 --hours 49
-        the config-3 ensemble (256 replicates, 30.6M agents) through the run loop, hours
+        the 256-replicate ensemble (30.6M agents) through the run loop, hours
         1..hours-1
     python -m epirust_gb300.profile_cases mlp-train --steps 30 [--members M]
         the surrogate network 8 -> 512 x 3 -> 600 (M members in one handle), batch 256, on a
@@ -26,13 +26,13 @@ import time
 import numpy as np
 
 HERE = os.path.dirname(os.path.abspath(__file__))
-C2 = os.path.join(os.path.dirname(HERE), "tests", "golden", "c2_small_pox_1m.json")
+WORLD_1M = os.path.join(os.path.dirname(HERE), "tests", "golden", "small_pox_1m_2500.json")
 
 
 def tick(args) -> dict:
     from .engine import Config, Epidemiology
 
-    with open(C2) as f:
+    with open(WORLD_1M) as f:
         cfg = json.load(f)
     cfg["population"]["Auto"]["number_of_agents"] = args.agents
     cfg["geography_parameters"]["grid_size"] = args.grid
@@ -51,11 +51,11 @@ def tick(args) -> dict:
 
 
 def run(args) -> dict:
-    """The config-2 run loop (1M agents, 2,500 grid, 4,800 h, lockdown, vaccination and the
+    """The 1M-agent run loop (2,500 grid, 4,800 h, lockdown, vaccination and the
     hospital build): the workload of bench.py's step, once, at the launch shape given."""
     from .engine import Config, Epidemiology
 
-    with open(C2) as f:
+    with open(WORLD_1M) as f:
         cfg = json.load(f)
     eng = Epidemiology(Config(json.dumps(cfg)))
     if args.shape:
@@ -69,7 +69,7 @@ def run(args) -> dict:
 
 
 def ensemble(args) -> dict:
-    """The config-3 ensemble (256 replicates, 10k-500k agents) through the run loop for
+    """The 256-replicate ensemble (10k-500k agents each) through the run loop for
     hours 1..hours-1."""
     from .engine import Ensemble
     from .workloads import ensemble_params

@@ -61,7 +61,7 @@ def test_ensemble_rerun_from_saved_state_repeats(gpu):
 
 
 def test_config3_shapes_small(gpu):
-    """The config-3 generator (log-uniform populations, sqrt grids) at 16 small replicates."""
+    """The 256-replicate generator (log-uniform populations, sqrt grids) at 16 small replicates."""
     from epirust_gb300 import Ensemble, Epidemiology
     from epirust_gb300.workloads import ensemble_params
 

@@ -159,9 +159,9 @@ def test_run_loop_parity(gpu, oracle_mod, name):
     eng.check_invariants()
 
 
-def test_c1_full_run_parity(gpu, oracle_mod):
-    """Config 1 (10k agents, 250 grid, small pox, 2,400 h): every hourly row equal."""
-    cfg = golden("c1_small_pox_10k.json")
+def test_small_pox_10k_full_run_parity(gpu, oracle_mod):
+    """The 10k-agent / 250-grid small-pox run (2,400 h): every hourly row equal."""
+    cfg = golden("small_pox_10k_250.json")
     eng, sim = _engine(cfg), _oracle(oracle_mod, cfg)
     got = _engine_rows(eng.run())
     want = rows_to_array(sim.run(1, cfg["hours"], interventions=True, stop=True))
@@ -222,8 +222,8 @@ def test_records_roundtrip(gpu, oracle_mod):
 
 
 def test_full_size_world_first_day_parity(gpu, oracle_mod):
-    """Config 2 at full size (1M agents, 2,500 grid): the first 30 hours equal the oracle."""
-    cfg = golden("c2_small_pox_1m.json")
+    """The 1M-agent / 2,500-grid world: the first 30 hours equal the oracle."""
+    cfg = golden("small_pox_1m_2500.json")
     eng, sim = _engine(cfg), _oracle(oracle_mod, cfg)
     got = _engine_rows(eng.simulate_hours(1, 30))
     want = rows_to_array(sim.run(1, 31, interventions=False, stop=False))
@@ -233,8 +233,8 @@ def test_full_size_world_first_day_parity(gpu, oracle_mod):
 
 
 def test_full_size_run_properties(gpu):
-    """Config 2 end to end at full size: invariants that hold whatever the trajectory."""
-    cfg = golden("c2_small_pox_1m.json")
+    """The 1M-agent / 2,500-grid run end to end: invariants that hold whatever the trajectory."""
+    cfg = golden("small_pox_1m_2500.json")
     eng = _engine(cfg)
     rows = eng.run()
     arr = _engine_rows(rows)

@@ -84,7 +84,7 @@ def test_config_parse_matches_reference_fixture(engine_built):
 def test_config_parse_equals_oracle_parse(engine_built, oracle_mod):
     from epirust_gb300 import Config
 
-    for cfg in (golden("c1_small_pox_10k.json"), golden("c2_small_pox_1m.json"), golden("auto_pop_config.json")):
+    for cfg in (golden("small_pox_10k_250.json"), golden("small_pox_1m_2500.json"), golden("auto_pop_config.json")):
         a = Config(json.dumps(cfg)).params
         b = oracle_mod.params_from_config(cfg)
         assert bytes(a) == bytes(b)
@@ -165,7 +165,7 @@ WORLDS = [
     make_config(n=1000, grid=80, seed=3),
     make_config(n=5000, grid=120, seed=11, pt=0.9, working=0.95, starting=(3, 3, 3, 10),
                 interventions=[{"Lockdown": {"at_number_of_infections": 5, "essential_workers_population": 0.3}}]),
-    golden("c1_small_pox_10k.json"),
+    golden("small_pox_10k_250.json"),
     make_config(n=24000, grid=250, seed=2**40 + 17, starting=(0, 0, 0, 37)),
 ]
 
@@ -191,7 +191,7 @@ def test_world_build_full_size_properties(engine_built):
     from epirust_gb300 import Config
     from epirust_gb300.engine import world_build
 
-    cfg = golden("c2_small_pox_1m.json")
+    cfg = golden("small_pox_1m_2500.json")
     recs, geo = world_build(Config(json.dumps(cfg)).params)
     n = len(recs)
     assert n == 1_000_000
