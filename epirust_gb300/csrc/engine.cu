@@ -1348,6 +1348,36 @@ int epi_geography_increase_hospital_size(epi_geography* geo, uint32_t grid_size)
     return EPI_OK;
 }
 
+int epi_interventions_replay(const epi_params* p, const epi_counts* rows, uint32_t n, uint32_t* applied,
+                             uint8_t* guard) {
+    if (!p || (n && (!rows || !applied))) return EPI_ERR_ARG;
+    const std::string bad = validate_params(*p);
+    if (!bad.empty()) { g_create_error = bad; return EPI_ERR_CONFIG; }
+    epi_geography geo = define_geography(p->grid_size);
+    resize_hospital(geo, (int32_t)p->number_of_agents, 0.002, p->hospital_beds_percentage);
+    const epi_geography geo0 = geo;
+    InterventionState st;
+    uint32_t ivn = 0;  // the device guard's new-infections figure
+    for (uint32_t k = 0; k < n; ++k) {
+        const epi_counts& c = rows[k];
+        if (guard) {  // k_piece_end's verdict on this row, from the thresholds pushed before it
+            uint8_t fire = 0;
+            if (c.hour % 24u == 0u) {
+                const GuardParams g = guard_params(*p, st, geo.hospital);
+                const uint32_t fresh = c.infected > ivn ? c.infected - ivn : 0u;
+                ivn = fresh;
+                fire = ((g.flags & 1u) && c.infected > g.lock_threshold) || ((g.flags & 2u) && fresh >= g.spread_threshold) ||
+                       ((g.flags & 4u) && c.hospitalized >= g.occ_threshold);
+            }
+            guard[k] = fire;
+        }
+        const InterventionActions a = decide_interventions(*p, st, c, geo.hospital);
+        if (a.grow_hospital) geo.hospital = grown_hospital(geo0);
+        applied[k] = a.applied;
+    }
+    return EPI_OK;
+}
+
 double epi_disease_transmission_rate(const epi_params* p, uint32_t day) {
     switch (rate_class(p->regular_transmission_start_day, p->high_transmission_start_day, p->last_day, day)) {
         case 1: return p->regular_transmission_rate;

@@ -81,6 +81,18 @@ def define_geography(grid_size: int) -> EpiGeography:
     return g
 
 
+def interventions_replay(params: EpiParams, rows: np.ndarray) -> tuple[np.ndarray, np.ndarray]:
+    """process_interventions' triggers on the host over hourly counts rows (COUNTS_DTYPE, in
+    the order the run loop offers them): per row the EPI_IV_* bits that fire, and whether the
+    run loop's device guard would mark that row."""
+    rows = np.ascontiguousarray(rows, dtype=COUNTS_DTYPE)
+    applied = np.zeros(len(rows), dtype=np.uint32)
+    guard = np.zeros(len(rows), dtype=np.uint8)
+    check(lib().epi_interventions_replay(C.byref(params), rows.ctypes.data, len(rows), applied.ctypes.data,
+                                         guard.ctypes.data))
+    return applied, guard
+
+
 def read_population_csv(path: str) -> np.ndarray:
     """Population::Csv rows as flags (bit 0 working, bit 1 public transport)."""
     n = C.c_uint32(0)

@@ -171,6 +171,16 @@ int epi_resize_hospital(epi_geography* geo, int32_t number_of_agents,
  * its start corner and ends at (grid_size, grid_size). */
 int epi_geography_increase_hospital_size(epi_geography* geo, uint32_t grid_size);
 
+/* The trigger logic of process_interventions (allocation_map.rs:306-337 with
+ * interventions/{vaccination,lockdown,hospital}.rs) on the host alone, for checks without a
+ * device: from a fresh intervention state the rows are offered in order, as the run loop
+ * offers every hour's counts.  applied[k] gets the EPI_IV_* bits that fire at rows[k].
+ * guard[k] (may be NULL) gets 1 where the run loop's device guard would mark rows[k] to halt
+ * its chain: a day boundary at which a lockdown or a hospital build is due, judged from the
+ * thresholds in force before that row. */
+int epi_interventions_replay(const epi_params* params, const epi_counts* rows, uint32_t n, uint32_t* applied,
+                             uint8_t* guard);
+
 /* Disease::get_current_transmission_rate / is_to_be_hospitalized
  * (common/src/disease/mod.rs:88-99). */
 double epi_disease_transmission_rate(const epi_params* p, uint32_t infection_day);
