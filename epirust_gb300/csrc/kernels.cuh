@@ -141,7 +141,16 @@ __device__ uint32_t block_first_vacant(const DevParams& P, const PlaneView& pl) 
     return pack_xy(h.x0 + (int32_t)(c % w), h.y0 + (int32_t)(c / w));
 }
 
-// Hours 1..6 (SLEEP_START_TIME..=SLEEP_END_TIME, citizen/mod.rs:244-248).
+// Hours 1..6 (SLEEP_START_TIME..=SLEEP_END_TIME, citizen/mod.rs:244-248).  A single world
+// takes its chunks kSleepBatch at a time with all their state loads in flight together (the
+// kernel is one load and a compare per agent, so one load round per chunk set its time).
+constexpr uint32_t kSleepBatch = 4;
+
+__device__ __forceinline__ void sleep_agent(uint2* __restrict__ st, uint32_t slot, bool valid, uint32_t s, uint32_t* sh) {
+    if (valid && st_ws(s) != EPI_WS_HOSPITAL_STAFF && st_area(s) != kHome) st[slot].x = with_area(s, kHome);
+    count_into(sh, valid, count_bin(s));
+}
+
 __global__ void __launch_bounds__(kThreads) k_sleep(const DevParams* __restrict__ Pall, const uint32_t* __restrict__ chunk_rep,
                                                     uint32_t n_chunks, uint2* __restrict__ st, HourArgs ha) {
     __shared__ uint32_t sh[8];
@@ -150,7 +159,31 @@ __global__ void __launch_bounds__(kThreads) k_sleep(const DevParams* __restrict_
     const HourRow hr = hour_row(ha);
     BlockRep br;
     bool ended = false;  // run_ended of the block's replicate (its prev row is fixed during the launch)
-    const uint32_t grp = chunk_rep ? kEnsembleChunkGroup : kWorldChunkGroup;  // chunks per stride step
+    if (!chunk_rep) {
+        if (blockIdx.x < n_chunks) {
+            switch_rep(br, 0u, Pall, sP, sh, row_ptr(ha, hr.row));
+            ended = run_ended(prev_ptr(ha, hr.row), 0u);
+        }
+        if (blockIdx.x < n_chunks && sP.active && !ended) {
+            for (uint32_t c0 = blockIdx.x; c0 < n_chunks; c0 += kSleepBatch * gridDim.x) {
+                uint32_t sv[kSleepBatch];
+#pragma unroll
+                for (uint32_t q = 0; q < kSleepBatch; ++q) {
+                    const uint32_t c = c0 + q * gridDim.x, slot = c * kChunk + threadIdx.x;
+                    sv[q] = (c < n_chunks && slot < sP.n) ? st[slot].x : 0u;  // slot = agent (agent_off 0)
+                }
+#pragma unroll
+                for (uint32_t q = 0; q < kSleepBatch; ++q) {
+                    const uint32_t c = c0 + q * gridDim.x, slot = c * kChunk + threadIdx.x;
+                    if (c >= n_chunks) break;  // block-uniform
+                    sleep_agent(st, slot, slot < sP.n, sv[q], sh);
+                }
+            }
+        }
+        flush_rep(br, sh, row_ptr(ha, hr.row));
+        return;
+    }
+    const uint32_t grp = kEnsembleChunkGroup;  // chunks per stride step
     for (uint32_t c = blockIdx.x * grp, k = 0; c < n_chunks;
          c = (++k < grp) ? c + 1u : c + (gridDim.x - 1u) * grp + 1u, k = (k < grp) ? k : 0u) {
         const uint32_t r = chunk_rep ? chunk_rep[c] : 0u;
@@ -161,15 +194,7 @@ __global__ void __launch_bounds__(kThreads) k_sleep(const DevParams* __restrict_
         if (!sP.active || ended) continue;
         const uint32_t slot = c * kChunk + threadIdx.x;
         const bool valid = slot - sP.agent_off < sP.n;
-        uint32_t s = 0;
-        if (valid) {
-            s = st[slot].x;
-            if (st_ws(s) != EPI_WS_HOSPITAL_STAFF && st_area(s) != kHome) {
-                s = with_area(s, kHome);
-                st[slot].x = s;
-            }
-        }
-        count_into(sh, valid, count_bin(s));
+        sleep_agent(st, slot, valid, valid ? st[slot].x : 0u, sh);
     }
     flush_rep(br, sh, row_ptr(ha, hr.row));
 }
