@@ -35,10 +35,12 @@ def grid_for(agents: int, density: float = 0.16) -> int:
 def train_on_abm(runs: int = 4096, held_out: int = 512, agents: int = 100_000, days: int = 100,
                  members: int = 5, steps: int = 3000, seed: int = 4, hidden: int = 512, hidden_layers: int = 3,
                  batch: int = 256, abm_batch: int = 512, per_agents: int = 100_000, curves: np.ndarray | None = None,
-                 noise_runs: int = 128):
+                 noise_runs: int = 128, mean_points: int = 128, mean_replicates: int = 8):
     """curves: ABM curves of this design computed before (skips the ABM stage).  noise_runs
     held-out points are simulated again with other seeds to measure the ABM's own peak-height
-    spread, the floor of any surrogate's error against single runs."""
+    spread, the floor of any surrogate's error against single runs.  mean_points held-out
+    points are run mean_replicates more times and the network's peak height is judged against
+    the mean of those runs (the ABM ensemble mean, which is what a sweep compares)."""
     grid = grid_for(agents)
     hours = 24 * days + 1
     u = latin_hypercube(runs, len(PARAMS), seed)
@@ -68,6 +70,27 @@ def train_on_abm(runs: int = 4096, held_out: int = 512, agents: int = 100_000, d
                 for i, d in enumerate(denormalise(xte[:n_rep]))]
     pe_rep = relative_peak_error(simulate_curves(rep_cfgs, days, batch=abm_batch), yte[:n_rep], days) if n_rep else None
     t_rep = time.perf_counter() - t0
+    # the network against the ABM ensemble mean of held-out points (fresh seeds)
+    n_mean = min(mean_points, held_out)
+    ens_info = None
+    if n_mean and mean_replicates:
+        t0 = time.perf_counter()
+        mean_cfgs = [config_for(d, agents, grid, hours, seed=seed * 1_000_003 + 700_000 + 97 * i + r, per_agents=per_agents)
+                     for i, d in enumerate(denormalise(xte[:n_mean])) for r in range(mean_replicates)]
+        runs_m = simulate_curves(mean_cfgs, days, batch=abm_batch).reshape(n_mean, mean_replicates, -1)
+        ens_mean = runs_m.mean(axis=1)
+        pe_mean = relative_peak_error(mean_pred[:n_mean], ens_mean, days)
+        # a single ABM run against the same mean (leave-one-out), for scale
+        loo = np.stack([(ens_mean * mean_replicates - runs_m[:, r]) / (mean_replicates - 1) for r in range(mean_replicates)],
+                       axis=1) if mean_replicates > 1 else None
+        pe_single = (np.concatenate([relative_peak_error(runs_m[:, r], loo[:, r], days) for r in range(mean_replicates)])
+                     if loo is not None else None)
+        ens_info = {
+            "points": n_mean, "replicates": mean_replicates, "s": time.perf_counter() - t0,
+            "median": float(np.median(pe_mean)), "p90": float(np.quantile(pe_mean, 0.9)),
+            "within_5pct": float(np.mean(pe_mean <= 0.05)),
+            "single_run_vs_mean_of_others_median": float(np.median(pe_single)) if pe_single is not None else None,
+            "note": "network peak height against the mean of mean_replicates fresh ABM runs per held-out point"}
     samples = members * steps * batch
     flop = 3.0 * _flops(len(PARAMS), hidden, hidden_layers, 6 * days) * samples  # forward + backward ~ 3x forward
     info = {
@@ -85,6 +108,8 @@ def train_on_abm(runs: int = 4096, held_out: int = 512, agents: int = 100_000, d
             "runs": n_rep, "median": float(np.median(pe_rep)), "p90": float(np.quantile(pe_rep, 0.9)),
             "within_5pct": float(np.mean(pe_rep <= 0.05)), "s": t_rep,
             "note": "the same held-out parameters run again with other seeds: the ABM's own peak-height spread"}
+    if ens_info is not None:
+        info["held_out_peak_rel_err_vs_abm_mean"] = ens_info
     info["curves"] = y
     return net, info
 
