@@ -2030,6 +2030,9 @@ extern "C" int epi_tick_hour_noalloc(const epi_params* params, uint32_t hour, ui
         return noalloc_fail(EPI_ERR_ARG, "epi_tick_hour_noalloc: null pointer argument");
     if (reinterpret_cast<uintptr_t>(state) % 8 != 0)
         return noalloc_fail(EPI_ERR_ARG, "epi_tick_hour_noalloc: state must be 8-byte aligned (two words per agent)");
+    // the neighbourhood reads take each plane row in aligned 32-bit words
+    if (reinterpret_cast<uintptr_t>(plane) % 4 != 0)
+        return noalloc_fail(EPI_ERR_ARG, "epi_tick_hour_noalloc: plane must be 4-byte aligned");
     const std::string bad = validate_params(*params);
     if (!bad.empty()) return noalloc_fail(EPI_ERR_CONFIG, bad);
     const uint32_t n = params->number_of_agents;

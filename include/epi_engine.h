@@ -392,7 +392,7 @@ int epi_ensemble_hour_bytes(const epi_ensemble* e, uint32_t hour, double* bytes)
  *   work_start_at[n]  hospital staff schedule
  *   plane[(G+3)^2+16] one byte per cell with a one-cell border: cell (x, y) at
  *                     (y+1)*(G+3) + x+1; 0 vacant, 1 occupied, 2/3 infectious at the regular /
- *                     high rate; border and slack bytes zero
+ *                     high rate; border and slack bytes zero.  4-byte aligned.
  *   counts[8]         out: S, E, I, H, R, D of this hour in counts[0..5]
  * hospital_grown = 1 once BuildNewHospital has fired.  The call is issued on cuda_stream
  * (NULL = the legacy default stream) and returns after the hour has finished.  The first call

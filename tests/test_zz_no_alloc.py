@@ -21,6 +21,7 @@ from helpers import COVID_FAST, make_config
 pytestmark = pytest.mark.gpu
 
 EPI_ERR_CAPACITY = 2
+EPI_ERR_ARG = 6
 
 
 def _rate_class(p, day):
@@ -158,3 +159,8 @@ def test_noalloc_rejects_worlds_beyond_its_scratch(gpu):
     rc = lib().epi_tick_hour_noalloc(C.byref(p), 7, 0, ptr, ptr, ptr, ptr, ptr, ptr, ptr, None)
     assert rc == EPI_ERR_CAPACITY
     assert b"fixed maximum" in lib().epi_engine_last_error(None)
+    # a plane that is not 4-byte aligned is refused before any device work
+    small = Config(json.dumps(make_config(n=500, grid=60))).params
+    rc = lib().epi_tick_hour_noalloc(C.byref(small), 7, 0, ptr, ptr, ptr, ptr, ptr, ptr + 1, ptr, None)
+    assert rc == EPI_ERR_ARG
+    assert b"4-byte aligned" in lib().epi_engine_last_error(None)
