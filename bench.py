@@ -162,9 +162,23 @@ def cpu_baseline(cfg: dict, records, seconds: float = 12.0, max_hours: int = 240
         hours += 1
     dt = time.perf_counter() - t0
     n = len(records)
-    return {"value": n * hours / dt, "unit": METRIC, "cores": threads, "kind": "port",
-            "sample": f"oracle/o2.c (reference data flow: FNV hash map, threaded map phase, serial "
-                      f"resolve) on the same {n}-agent world, hours 1..{hours} ({dt:.1f} s)"}
+    out = {"value": n * hours / dt, "unit": METRIC, "cores": threads, "kind": "port",
+           "sample": f"oracle/o2.c (reference data flow: FNV hash map, threaded map phase, serial "
+                     f"resolve) on the same {n}-agent world, hours 1..{hours} ({dt:.1f} s)"}
+    # the same port with the reference CLI's default thread count (-t 4), and the scalar
+    # bit-exact oracle O1 on one thread, each over a short sample of the same hours
+    variants = {}
+    for name, make in (("o2_threads_4", lambda: oracle.O2(params, records, threads=4)),
+                       ("o1_single_thread", lambda: oracle.O1(params, records))):
+        sim = make()
+        t0 = time.perf_counter()
+        h = 0
+        while h < max_hours and (time.perf_counter() - t0) < seconds / 4:
+            sim.run(1 + h, 2 + h, interventions=True, stop=False)
+            h += 1
+        variants[name] = {"value": n * h / (time.perf_counter() - t0), "hours": h}
+    out["variants"] = variants
+    return out
 
 
 def run_reference(args, cfg):
