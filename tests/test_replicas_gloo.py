@@ -53,4 +53,3 @@ def test_two_rank_replica_aggregation():
     assert len(set(seeds)) == 2  # every rank simulates a different world
     value = agent_hours / (ms_max / 1000.0)  # the job's agent-hours/s
     assert value == pytest.approx(2.4e10)
-
