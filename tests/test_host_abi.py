@@ -90,6 +90,21 @@ def test_config_parse_equals_oracle_parse(engine_built, oracle_mod):
         assert bytes(a) == bytes(b)
 
 
+def test_disease_overrides_are_accepted_and_unused(engine_built):
+    """Config::disease_overrides (common/src/config/mod.rs:49) is parsed by the reference but
+    read nowhere in the engine: a config carrying one gives the same parameters."""
+    import ctypes as C
+
+    from epirust_gb300 import Config
+
+    cfg = make_config()
+    with_override = dict(cfg)
+    with_override["disease_overrides"] = [{"population_param": "age", "values": ["60-64", "65-69"],
+                                           "disease": dict(cfg["disease"], death_rate=0.3)}]
+    a, b = Config(json.dumps(cfg)).params, Config(json.dumps(with_override)).params
+    assert C.string_at(C.addressof(a), C.sizeof(a)) == C.string_at(C.addressof(b), C.sizeof(b))
+
+
 def test_config_defaults_and_errors(engine_built):
     from epirust_gb300 import Config, EpiError
 
