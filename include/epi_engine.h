@@ -229,7 +229,7 @@ int epi_engine_set_stream(epi_engine* h, void* cuda_stream);
 int epi_engine_simulate(epi_engine* h, uint32_t hour, epi_counts* out);
 
 /* n consecutive hours first_hour .. first_hour+n-1 with no interventions in between,
- * issued as one CUDA graph (or one persistent launch); out gets n rows. */
+ * issued as captured CUDA graphs of whole days launched back to back; out gets n rows. */
 int epi_engine_simulate_hours(epi_engine* h, uint32_t first_hour, uint32_t n, epi_counts* out);
 
 /* CitizenLocationMap::process_interventions (engine/src/allocation_map.rs:306-337) with
