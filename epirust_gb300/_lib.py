@@ -95,7 +95,7 @@ COUNTS_DTYPE = np.dtype([(k, "<u4") for k in
 # Every symbol include/epi_engine.h declares.
 EXPORTS = [
     "epi_params_from_json", "epi_define_geography", "epi_resize_hospital", "epi_geography_increase_hospital_size", "epi_disease_transmission_rate",
-    "epi_disease_is_to_be_hospitalized", "epi_interventions_replay", "epi_world_build", "epi_engine_create", "epi_engine_create_json",
+    "epi_disease_is_to_be_hospitalized", "epi_interventions_replay", "epi_outputs_write", "epi_world_build", "epi_engine_create", "epi_engine_create_json",
     "epi_engine_create_from_records", "epi_engine_destroy", "epi_engine_last_error", "epi_engine_set_stream",
     "epi_engine_simulate", "epi_engine_simulate_hours", "epi_engine_process_interventions", "epi_engine_lock_city",
     "epi_engine_unlock_city", "epi_engine_vaccinate", "epi_engine_increase_hospital_size", "epi_engine_run",
@@ -162,6 +162,7 @@ def lib():
     _sig(L, "epi_disease_transmission_rate", C.c_double, [P(EpiParams), C.c_uint32])
     _sig(L, "epi_disease_is_to_be_hospitalized", C.c_int, [P(EpiParams), C.c_uint32])
     _sig(L, "epi_interventions_replay", C.c_int, [P(EpiParams), V, C.c_uint32, V, V])
+    _sig(L, "epi_outputs_write", C.c_int, [C.c_char_p, C.c_char_p, P(EpiParams), V, C.c_uint32])
     _sig(L, "epi_world_build", C.c_int, [P(EpiParams), V, C.c_size_t, P(EpiGeography)])
     _sig(L, "epi_engine_create", C.c_int, [P(EpiParams), P(V)])
     _sig(L, "epi_engine_create_json", C.c_int, [C.c_char_p, C.c_uint64, P(V)])

@@ -1378,6 +1378,22 @@ int epi_interventions_replay(const epi_params* p, const epi_counts* rows, uint32
     return EPI_OK;
 }
 
+int epi_outputs_write(const char* dir, const char* engine_id, const epi_params* p, const epi_counts* rows, uint32_t n) {
+    if (!dir || !engine_id || !p || (n && !rows)) return EPI_ERR_ARG;
+    const std::string bad = validate_params(*p);
+    if (!bad.empty()) { g_create_error = bad; return EPI_ERR_CONFIG; }
+    epi_geography geo = define_geography(p->grid_size);
+    resize_hospital(geo, (int32_t)p->number_of_agents, 0.002, p->hospital_beds_percentage);
+    const epi_geography geo0 = geo;
+    InterventionState st;
+    for (uint32_t k = 0; k < n; ++k)
+        if (decide_interventions(*p, st, rows[k], geo.hospital).grow_hospital) geo.hospital = grown_hospital(geo0);
+    std::string err;
+    const int rc = write_outputs(dir, engine_id, std::vector<epi_counts>(rows, rows + n), st.reports, err);
+    if (rc) g_create_error = err;
+    return rc;
+}
+
 double epi_disease_transmission_rate(const epi_params* p, uint32_t day) {
     switch (rate_class(p->regular_transmission_start_day, p->high_transmission_start_day, p->last_day, day)) {
         case 1: return p->regular_transmission_rate;

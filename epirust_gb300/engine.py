@@ -93,6 +93,14 @@ def interventions_replay(params: EpiParams, rows: np.ndarray) -> tuple[np.ndarra
     return applied, guard
 
 
+def write_outputs_for_rows(directory: str, engine_id: str, params: EpiParams, rows: np.ndarray) -> None:
+    """The reference listeners' CSV and interventions JSON for hourly counts rows, without a
+    device (the interventions are replayed over the rows)."""
+    rows = np.ascontiguousarray(rows, dtype=COUNTS_DTYPE)
+    check(lib().epi_outputs_write(os.fsencode(directory), engine_id.encode(), C.byref(params), rows.ctypes.data,
+                                  len(rows)))
+
+
 def read_population_csv(path: str) -> np.ndarray:
     """Population::Csv rows as flags (bit 0 working, bit 1 public transport)."""
     n = C.c_uint32(0)

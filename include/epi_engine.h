@@ -181,6 +181,16 @@ int epi_geography_increase_hospital_size(epi_geography* geo, uint32_t grid_size)
 int epi_interventions_replay(const epi_params* params, const epi_counts* rows, uint32_t n, uint32_t* applied,
                              uint8_t* guard);
 
+/* The listeners' files for a run's rows, without a device: CsvListener's
+ * <dir>/output/simulation_<engine_id>_<UTC YYYY-MM-DDTHH:MM:SS>.csv (header hour, susceptible,
+ * exposed, infected, hospitalized, recovered, deceased; one line per row) and
+ * InterventionReporter's ..._interventions.json, whose reports come from replaying the
+ * intervention triggers over the rows (util.rs:36-43, csv_service.rs:44-71,
+ * intervention_reporter.rs:52-58).  epi_engine_write_outputs writes the same files from an
+ * engine's own run. */
+int epi_outputs_write(const char* dir, const char* engine_id, const epi_params* params, const epi_counts* rows,
+                      uint32_t n);
+
 /* Disease::get_current_transmission_rate / is_to_be_hospitalized
  * (common/src/disease/mod.rs:88-99). */
 double epi_disease_transmission_rate(const epi_params* p, uint32_t infection_day);

@@ -2,7 +2,8 @@
 build; engine/src/allocation_map.rs:306-337) on the host, without a device: the reference's
 known-answer tests for engine/src/interventions/{lockdown,hospital,vaccination}.rs, the
 oracle's triggers on random count sequences, and the run loop's device guard, which must mark
-exactly the day-boundary rows at which a lockdown or a hospital build fires."""
+exactly the day-boundary rows at which a lockdown or a hospital build fires.  Also the
+listeners' output files (CsvListener, InterventionReporter) for a run's rows."""
 import json
 
 import numpy as np
@@ -119,3 +120,32 @@ def test_engine_triggers_equal_the_oracle_and_the_guard(engine_built, oracle_mod
     boundary = rows["hour"] % 24 == 0
     assert ((guard != 0) == (boundary & ((applied & (LOCK | HOSP)) != 0))).all()
     assert (applied & (LOCK | HOSP)).any()  # the sequences do exercise the triggers
+
+
+def test_listener_files_for_a_run(engine_built, tmp_path):
+    """CsvListener and InterventionReporter output for given rows: the file names of
+    output_file_format (util.rs:36-43), the csv header and one line per row, and the report
+    list serde writes (hour, intervention, data; compact JSON)."""
+    import glob
+    import os
+    import re
+
+    from epirust_gb300.engine import write_outputs_for_rows
+
+    cfg = _lockdown(threshold=20)
+    cfg["interventions"].append({"Vaccinate": {"at_hour": 30, "percent": 0.2}})
+    rows = _rows(*[(h, 100 - min(h, 30), 0, min(h, 30), 0, 0, 0) for h in range(1, 50)])
+    write_outputs_for_rows(str(tmp_path), "7", _params(cfg), rows)
+    files = sorted(os.path.basename(f) for f in glob.glob(str(tmp_path / "output" / "*")))
+    assert len(files) == 2
+    stamp = r"\d{4}-\d\d-\d\dT\d\d:\d\d:\d\d"
+    assert re.fullmatch(rf"simulation_7_{stamp}\.csv", files[0]), files
+    assert re.fullmatch(rf"simulation_7_{stamp}_interventions\.json", files[1]), files
+    lines = (tmp_path / "output" / files[0]).read_text().splitlines()
+    assert lines[0] == "hour,susceptible,exposed,infected,hospitalized,recovered,deceased"
+    assert lines[1:] == [",".join(str(int(v)) for v in r) for r in rows]
+    reports = json.loads((tmp_path / "output" / files[1]).read_text())
+    assert reports == [{"hour": 24, "intervention": "lockdown", "data": {"status": "locked_down"}},
+                       {"hour": 30, "intervention": "vaccination", "data": {}}]
+    text = (tmp_path / "output" / files[1]).read_text()
+    assert text == json.dumps(reports, separators=(",", ":"))
