@@ -13,7 +13,9 @@ The L2 (129 MB) is flushed between steps by writing a 512 MiB buffer; within a s
 1M-agent working set (~60 MB) is L2-resident by design.
 
 --impl reference times the CPU port of the reference's own tick data flow (hash map,
-threaded map phase, serial resolve; oracle/o2.c) on all host cores.  Under torchrun the
+threaded map phase, serial resolve; oracle/o2.c) on all host cores, over consecutive 24-hour
+windows of the same run from a world built by the oracle (the engine library is not loaded
+in that process); both arms print the same `config` object.  Under torchrun the
 engine runs as independent replicas (one per GPU, different seeds): the tick has no
 exchange step to shard.
 """
@@ -181,40 +183,68 @@ def cpu_baseline(cfg: dict, records, seconds: float = 12.0, max_hours: int = 240
     return out
 
 
+def workload_config(cfg: dict, world: int) -> dict:
+    """The `config` object of both arms' JSON lines (identical, so the two lines describe
+    one workload)."""
+    auto = cfg["population"]["Auto"]
+    return {
+        "workload": "plain single-engine tick: 1M agents, 2500 grid, 4800 h, lockdown + vaccination + hospital "
+                    "build (tests/golden/small_pox_1m_2500.json); metric per agent-hour, so the CPU reference arm "
+                    "times consecutive windows of the same run and reports agent-hours/s over them",
+        "agents": int(auto["number_of_agents"]), "grid": int(cfg["geography_parameters"]["grid_size"]),
+        "hours": int(cfg["hours"]), "seed": int(cfg.get("seed", 0)),
+        "interventions": "lockdown at >1000 infected (10% essential), vaccinate 20% of susceptible at hour 2400, "
+                         "hospital build at 70% occupancy",
+        "parallelism": f"replicas{world}",
+        "l2": "GPU arm: flushed between steps (512 MiB write); inputs L2-resident within a step",
+    }
+
+
 def run_reference(args, cfg):
+    """The reference's tick data flow on the host cores: oracle/o2.c (FNV hash map keyed by
+    cell, threaded map phase, serial resolve in hash order, swap) over the same world, built
+    by the oracle's own world build (oracle/o1.c) -- nothing of the engine library is loaded.
+    One step = the next `ref_hours` hours of one continuing run (interventions on), so the
+    warm-up and timed steps together cover hours 1 .. (warmup + steps) * ref_hours."""
     world, rank, _ = _dist()
     if rank != 0:
         return
-    from epirust_gb300 import Config
-    from epirust_gb300.engine import world_build
     from oracle import oracle
 
-    records, _ = world_build(Config(json.dumps(cfg)).params)
-    threads = os.cpu_count() or 1
+    oracle.build()
     params = oracle.params_from_config(cfg)
+    t0 = time.perf_counter()
+    records = oracle.O1(params).export()
+    build_s = time.perf_counter() - t0
+    threads = os.cpu_count() or 1
     n = len(records)
     sample_hours = args.ref_hours
+    sim = oracle.O2(params, records, threads=threads)
+    hour = [1]
 
     def step():
-        sim = oracle.O2(params, records, threads=threads)
+        first = hour[0]
         t0 = time.perf_counter()
-        sim.run(1, 1 + sample_hours, interventions=True, stop=False, keep_rows=False)
+        sim.run(first, first + sample_hours, interventions=True, stop=False, keep_rows=False)
+        hour[0] = first + sample_hours
         return time.perf_counter() - t0
 
     for _ in range(args.warmup):
         step()
+    timed_first = hour[0]
     times = [step() for _ in range(args.steps)]
     total = sum(times)
     value = n * sample_hours * args.steps / total
+    sample = (f"oracle/o2.c on {threads} threads, {n}-agent world from the oracle's world build ({build_s:.1f} s, "
+              f"untimed); timed hours {timed_first}..{hour[0] - 1} of one run, {sample_hours} h per step, after "
+              f"{args.warmup} warm-up steps")
     line = {
         "impl": "reference", "metric": METRIC, "value": value, "unit": METRIC, "n_gpus": world, "steps": args.steps,
         "warmup": args.warmup, "ms_per_step": 1000 * total / args.steps, "higher_is_better": True,
         "scaling": "weak", "vs_baseline": None, "dtype": "u32", "data": "synthetic",
-        "config": {"workload": "plain single-engine tick, 1M agents, 2500 grid (first "
-                               f"{sample_hours} h of the 4800 h run per step)", "parallelism": "cpu threads",
-                   "threads": threads},
-        "cpu_baseline": {"value": value, "unit": METRIC, "cores": threads, "kind": "port",
-                         "sample": f"hours 1..{sample_hours} of the {n}-agent world per step"},
+        "config": workload_config(cfg, world),
+        "hours_per_step": sample_hours,
+        "cpu_baseline": {"value": value, "unit": METRIC, "cores": threads, "kind": "port", "sample": sample},
         "e2e": {"value": value, "unit": METRIC, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
     }
     print(json.dumps(line), flush=True)
@@ -307,16 +337,17 @@ def run_batched(args, stream, flush) -> dict:
 def run_surrogate(args) -> dict:
     """Surrogate training on GPU-ABM ensembles (4,096 Latin-hypercube runs of 100,000 agents,
     100 days, 5 MLP members 8 -> 512 x 3 -> 600 trained with Adam in BF16 on the tensor cores)
-    and the screened sweep (65,536 candidates, the best `sweep_keep` re-run at 1,000,000
-    agents with 8 replicates each, the same ABM budget on unscreened candidates)."""
+    and the screened sweep (65,536 candidates, the best `sweep_keep` and the fallback
+    candidates where the members disagree re-run at 1,000,000 agents with 8 replicates each;
+    an ABM-only sweep measured on the same budget of unscreened candidates)."""
     from epirust_gb300.sweep import screened_sweep, train_on_abm
 
     net, train = train_on_abm(runs=args.train_runs, held_out=args.train_runs // 8, steps=args.train_steps)
     train.pop("curves")
     sweep = screened_sweep(net, keep=args.sweep_keep, replicates=args.sweep_replicates)
     net.close()
-    sweep["note"] = ("abm_only_sweep_s_estimated = every candidate x replicates through the ABM at the rate "
-                     "measured for the re-run stage")
+    sweep["note"] = ("abm_only_sweep_s_extrapolated = every candidate x replicates through the ABM at the rate "
+                     "measured on its sample (abm_only_sample_runs unscreened runs, the screened sweep's budget)")
     return {"metric": "surrogate sweep speedup @<=5% peak err", "training": train, "sweep": sweep}
 
 
@@ -462,11 +493,8 @@ def run_gpu(args, cfg):
             "metric": METRIC, "value": value, "unit": METRIC, "n_gpus": world, "steps": args.steps,
             "warmup": args.warmup, "ms_per_step": ms_total / args.steps, "higher_is_better": True,
             "scaling": "weak", "vs_baseline": None, "dtype": "u32", "data": "synthetic",
-            "config": {"workload": "plain single-engine tick: 1M agents, 2500 grid, 4800 h, lockdown + "
-                                   "vaccination + hospital build (tests/golden/small_pox_1m_2500.json)",
-                       "agents": n, "grid": G, "hours_per_step": hours_per_step, "parallelism": f"replicas{world}",
-                       "l2": "flushed between steps (512 MiB write); inputs L2-resident within a step",
-                       "launch_shape": shape, "wall_s": wall},
+            "config": workload_config(cfg, world),
+            "hours_per_step": hours_per_step, "launch_shape": shape, "wall_s": wall,
             "roofline": {"bound": "hbm", "kernel": "k_decide", "achieved": achieved, "peak": peak, "unit": "GB/s",
                          "frac": achieved / peak, "peak_kind": peak_kind, "traffic": traffic,
                          "alg_bytes_per_launch": alg_bytes, "avg_launch_ms": avg_ms,
@@ -509,7 +537,7 @@ def main():
     ap.add_argument("--no-surrogate", action="store_true")
     ap.add_argument("--train-runs", type=int, default=4096)
     ap.add_argument("--train-steps", type=int, default=3000)
-    ap.add_argument("--sweep-keep", type=int, default=32)
+    ap.add_argument("--sweep-keep", type=int, default=256)
     ap.add_argument("--sweep-replicates", type=int, default=8)
     args = ap.parse_args()
     with open(args.config) as f:

@@ -318,7 +318,7 @@ using DecideKernel = void (*)(const DevParams*, const uint32_t*, uint32_t, const
                               HourArgs, int*);
 
 // Hours 2..6 of a day change nothing once hour 1 has sent everyone but hospital staff home
-// (routine, citizen/mod.rs:243-247, sets current_area = home_location and nothing else), so
+// (routine, citizen/mod.rs:244-248, sets current_area = home_location and nothing else), so
 // when the previous hour ran in the same chain the hour's kernel is skipped and its counts
 // row repeats the previous one.  (A piece that starts at hours 2..6 always starts a chain.)
 static bool sleep_hour_skipped(uint32_t first_hour, uint32_t k) {
@@ -2046,9 +2046,15 @@ extern "C" int epi_tick_hour_noalloc(const epi_params* params, uint32_t hour, ui
         return noalloc_fail(EPI_ERR_ARG, "epi_tick_hour_noalloc: null pointer argument");
     if (reinterpret_cast<uintptr_t>(state) % 8 != 0)
         return noalloc_fail(EPI_ERR_ARG, "epi_tick_hour_noalloc: state must be 8-byte aligned (two words per agent)");
-    // the neighbourhood reads take each plane row in aligned 32-bit words
+    // the neighbourhood reads take each plane row in aligned 32-bit words; the per-agent
+    // arrays and the counts are read and written as 32-bit words
     if (reinterpret_cast<uintptr_t>(plane) % 4 != 0)
         return noalloc_fail(EPI_ERR_ARG, "epi_tick_hour_noalloc: plane must be 4-byte aligned");
+    for (const void* w : {(const void*)pos, (const void*)home, (const void*)work, (const void*)work_start_at,
+                          (const void*)counts})
+        if (reinterpret_cast<uintptr_t>(w) % 4 != 0)
+            return noalloc_fail(EPI_ERR_ARG,
+                                "epi_tick_hour_noalloc: pos, home, work, work_start_at and counts must be 4-byte aligned");
     const std::string bad = validate_params(*params);
     if (!bad.empty()) return noalloc_fail(EPI_ERR_CONFIG, bad);
     const uint32_t n = params->number_of_agents;

@@ -211,7 +211,7 @@ static epi_area mk(int32_t x0, int32_t y0, int32_t x1, int32_t y1) {
 
 // define_geography (engine/src/geography/mod.rs:33-70): four vertical strips of
 // ceil(0.4G), ceil(0.2G), ceil(0.2G), ceil(0.1G) columns, each spanning rows 0..=G, and
-// the 2x2 / 10x10 tilings of area_factory (area.rs:186-208).
+// the 2x2 / 10x10 tilings of area_factory (area.rs:95-117).
 epi_geography define_geography(uint32_t grid_size) {
     const double g = (double)grid_size;
     const int32_t G = (int32_t)grid_size;

@@ -120,7 +120,7 @@ __device__ __forceinline__ void flush_rep(const BlockRep& br, uint32_t* sh, uint
     if (br.r != 0xFFFFFFFFu && threadIdx.x < 6 && sh[threadIdx.x]) atomicAdd(&counts[br.r * 8 + threadIdx.x], sh[threadIdx.x]);
 }
 
-// First vacant hospital cell of the snapshot in AreaIterator order (area.rs:221-237), found
+// First vacant hospital cell of the snapshot in AreaIterator order (area.rs:131-148), found
 // by the whole block; kNoAction when the hospital is full.
 __device__ uint32_t block_first_vacant(const DevParams& P, const PlaneView& pl) {
     __shared__ uint32_t best;

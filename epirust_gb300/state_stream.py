@@ -55,3 +55,39 @@ def read_state_stream(path: str):
                 y[agents] = (cell >> 16).astype(np.int32)
             letters = (codes >> 4) & 7
             yield hour, x.copy(), y.copy(), letters.copy()
+
+
+def citizen_uuid(agent: int) -> str:
+    """A stable citizen_id for agent index `agent`: the reference draws a random version-4 UUID
+    per citizen (Citizen::new, engine/src/citizen/mod.rs:66-75); here the index fills the low 62 bits
+    of a version-4, variant-1 UUID, so ids are unique, valid and the same in every run."""
+    v = (agent & ((1 << 62) - 1)) | (0x4 << 76) | (0x2 << 62)
+    h = f"{v:032x}"
+    return f"{h[:8]}-{h[8:12]}-{h[12:16]}-{h[16:20]}-{h[20:]}"
+
+
+def citizen_states_at_hr(hour: int, x, y, letters) -> dict:
+    """One CitizenStatesAtHr record (engine/src/models/events/citizen_state.rs:27-70) as the
+    reference's serde_json writes it: {"hr", "citizen_states": [{"citizen_id", "state",
+    "location": {"x", "y"}}]}, citizens in agent order."""
+    return {"hr": int(hour), "citizen_states": [
+        {"citizen_id": citizen_uuid(i), "state": LETTERS[int(l)], "location": {"x": int(a), "y": int(b)}}
+        for i, (a, b, l) in enumerate(zip(x, y, letters))]}
+
+
+def write_citizen_states_json(stream_path: str, out_path: str) -> int:
+    """Convert a state-stream file into the reference's message form: one CitizenStatesAtHr JSON
+    object per recorded hour, one per line (the payloads the reference's Kafka listener
+    publishes on its citizen-states topic, events_kafka_producer.rs:90-99).  Returns the
+    number of hours written."""
+    import json
+
+    hours = 0
+    with open(out_path, "w") as out:
+        for hour, x, y, letters in read_state_stream(stream_path):
+            if hour == 0:  # the keyframe: the state before the first recorded hour
+                continue
+            out.write(json.dumps(citizen_states_at_hr(hour, x, y, letters), separators=(",", ":")))
+            out.write("\n")
+            hours += 1
+    return hours

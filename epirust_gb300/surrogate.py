@@ -287,6 +287,47 @@ def screen(nets, candidates: np.ndarray, target: np.ndarray, keep: int, days: in
     return best, scores[best], flagged
 
 
+def member_peak_spread(nets, points: np.ndarray, days: int) -> np.ndarray:
+    """(max - min) / |mean| of the members' predicted infected peaks at each point."""
+    nets = [nets] if isinstance(nets, Surrogate) else list(nets)
+    if len(points) == 0:
+        return np.zeros(0)
+    preds = np.concatenate([n.predict_members(points) for n in nets])
+    peaks = np.stack([peak_height(p, days) for p in preds])
+    return (peaks.max(axis=0) - peaks.min(axis=0)) / np.maximum(np.abs(peaks.mean(axis=0)), 1e-12)
+
+
+def screen_with_fallback(nets, candidates: np.ndarray, target: np.ndarray, keep: int, days: int,
+                         peak_tolerance: float = 0.05, max_fallback: int | None = None):
+    """The surrogate screen with the ABM as its fallback.  Candidates are ranked by the members'
+    mean score and the best `keep` are kept.  Where the members disagree the mean cannot be
+    trusted, so a candidate outside the kept set is handed to the ABM when (a) at least one
+    member scores it within the kept set's worst mean score -- its rank depends on which
+    member is believed -- and (b) the members' predicted infected peaks spread by more than
+    peak_tolerance of their mean.  Those are taken most promising first (lowest member score),
+    at most max_fallback of them (default keep // 4).
+
+    Returns a dict: kept (indices), kept_scores, kept_flagged (mask over kept: members disagree
+    by more than peak_tolerance -- re-run by the ABM anyway), fallback (indices for the ABM),
+    uncertain (how many candidates met (a)), fallback_eligible (how many met (a) and (b))."""
+    nets = [nets] if isinstance(nets, Surrogate) else list(nets)
+    member_scores = np.concatenate([n.score_members(candidates, target) for n in nets])
+    mean_scores = member_scores.mean(axis=0)
+    order = np.argsort(mean_scores, kind="stable")
+    kept = order[:keep]
+    cut = mean_scores[kept[-1]] if len(kept) else -np.inf
+    outside = order[keep:]
+    best_member = member_scores[:, outside].min(axis=0)
+    uncertain = outside[best_member <= cut]
+    uncertain = uncertain[np.argsort(member_scores[:, uncertain].min(axis=0), kind="stable")]
+    spread_u = member_peak_spread(nets, candidates[uncertain], days)
+    eligible = uncertain[spread_u > peak_tolerance]
+    cap = keep // 4 if max_fallback is None else max_fallback
+    return {"kept": kept, "kept_scores": mean_scores[kept],
+            "kept_flagged": member_peak_spread(nets, candidates[kept], days) > peak_tolerance,
+            "fallback": eligible[:cap], "uncertain": int(len(uncertain)), "fallback_eligible": int(len(eligible))}
+
+
 def relative_peak_error(curves: np.ndarray, reference: np.ndarray, days: int) -> np.ndarray:
     p, q = peak_height(curves, days), peak_height(reference, days)
     return np.abs(p - q) / np.maximum(q, 1e-12)

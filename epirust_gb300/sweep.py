@@ -6,7 +6,9 @@ train_on_abm():  Latin-hypercube parameter points -> batched GPU-ABM runs -> dai
                  against the ABM and against the training-mean curve.
 screened_sweep(): a target curve from hidden parameters (ABM at full size), candidates scored
                  by the surrogate ensemble, the best re-run by the batched ABM with several
-                 replicates each, and the same ABM budget spent on unscreened candidates.
+                 replicates each together with the candidates the ABM takes over where the
+                 members disagree (the fallback), and an ABM-only sweep measured on the same
+                 budget of unscreened candidates.
 
 Times are wall-clock around calls that return after the device has finished (the ABM
 through epi_ensemble_run, the network through epi_mlp_*).
@@ -18,8 +20,8 @@ import time
 
 import numpy as np
 
-from .surrogate import (PARAMS, Surrogate, compartment_scaling, config_for, denormalise, latin_hypercube,
-                        relative_peak_error, screen, simulate_curves, uniform_candidates, unit_distance)
+from .surrogate import (PARAMS, Surrogate, screen_with_fallback, compartment_scaling, config_for, denormalise, latin_hypercube,
+                        relative_peak_error, simulate_curves, uniform_candidates, unit_distance)
 
 
 def _flops(in_dim: int, hidden: int, layers: int, out_dim: int) -> float:
@@ -116,7 +118,17 @@ def train_on_abm(runs: int = 4096, held_out: int = 512, agents: int = 100_000, d
 
 def screened_sweep(net, candidates: int = 65_536, keep: int = 256, replicates: int = 8, agents: int = 1_000_000,
                    days: int = 100, seed: int = 99, peak_tolerance: float = 0.05, abm_batch: int = 64,
-                   per_agents: int = 100_000):
+                   per_agents: int = 100_000, max_fallback: int | None = None):
+    """The surrogate-screened sweep and an ABM-only sweep of the same budget.
+
+    A target curve comes from the ABM at `agents` agents with hidden parameters (seed).  The
+    surrogate ensemble scores every candidate; the best `keep` are re-run by the batched ABM
+    with `replicates` replicates each, and so are the fallback candidates of
+    screen_with_fallback (outside the kept set, members disagreeing on their rank and on their
+    peak by more than peak_tolerance).  The sweep's answer is the re-run candidate whose
+    replicate-mean curve is closest to the target.  The ABM-only sweep spends the same number
+    of ABM runs on unscreened candidates (uniformly drawn): it is measured on that sample, and
+    its time for all `candidates` is extrapolated from the measured rate."""
     grid = grid_for(agents)
     hours = 24 * days + 1
     rng = np.random.default_rng(seed)
@@ -127,11 +139,13 @@ def screened_sweep(net, candidates: int = 65_536, keep: int = 256, replicates: i
     t_target = time.perf_counter() - t0
     cand = uniform_candidates(candidates, len(PARAMS), seed + 1)
 
-    # surrogate screen
+    # surrogate screen (and the candidates handed to the ABM because the members disagree)
     t0 = time.perf_counter()
-    best, best_scores, flagged = screen(net, cand, target, keep, days, peak_tolerance)
+    sc = screen_with_fallback(net, cand, target, keep, days, peak_tolerance, max_fallback)
     t_screen = time.perf_counter() - t0
-    sur_mean = net.predict(cand[best])
+    rerun = np.concatenate([sc["kept"], sc["fallback"]])
+    n_kept = len(sc["kept"])
+    sur_mean = net.predict(cand[rerun])
 
     def abm(points: np.ndarray, base_seed: int) -> np.ndarray:
         cfgs = [config_for(d, agents, grid, hours, seed=base_seed + 97 * i + r, per_agents=per_agents)
@@ -139,14 +153,15 @@ def screened_sweep(net, candidates: int = 65_536, keep: int = 256, replicates: i
         return simulate_curves(cfgs, days, batch=abm_batch).reshape(len(points), replicates, -1)
 
     t0 = time.perf_counter()
-    runs_s = abm(cand[best], 10_000)
+    runs_s = abm(cand[rerun], 10_000)
     t_abm_screened = time.perf_counter() - t0
     mean_s = runs_s.mean(axis=1)
     err_s = ((mean_s - target) ** 2).mean(axis=1)
     pick = int(np.argmin(err_s))
 
-    # the same ABM budget on unscreened candidates
-    rand_idx = np.random.default_rng(seed + 2).choice(candidates, keep, replace=False)
+    # the ABM-only sweep, measured on a sample of the same budget (unscreened candidates)
+    budget = len(rerun)
+    rand_idx = np.random.default_rng(seed + 2).choice(candidates, budget, replace=False)
     t0 = time.perf_counter()
     runs_r = abm(cand[rand_idx], 20_000)
     t_abm_random = time.perf_counter() - t0
@@ -154,29 +169,39 @@ def screened_sweep(net, candidates: int = 65_536, keep: int = 256, replicates: i
     err_r = ((mean_r - target) ** 2).mean(axis=1)
     pick_r = int(np.argmin(err_r))
 
-    # surrogate vs ABM ensemble mean at the screened candidates (the stated error criterion)
+    # the stated criterion: surrogate peak height against the ABM replicate mean, at sweep scale
     peak_err = relative_peak_error(sur_mean, mean_s, days)
-    per_run_s = t_abm_screened / (keep * replicates)
-    abm_only_s = candidates * replicates * per_run_s  # every candidate through the ABM at the measured rate
+    abm_only_s = candidates * replicates * t_abm_random / (budget * replicates)
     screened_s = t_screen + t_abm_screened
+    top = np.argsort(err_s)[:8]
+    top_r = np.argsort(err_r)[:8]
     return {
-        "candidates": candidates, "keep": keep, "replicates": replicates, "agents": agents, "grid": grid,
+        "candidates": candidates, "keep": n_kept, "replicates": replicates, "agents": agents, "grid": grid,
         "days": days, "target_abm_s": t_target, "screen_s": t_screen, "abm_screened_s": t_abm_screened,
-        "abm_random_s": t_abm_random, "abm_run_s": per_run_s,
-        "abm_agent_hours_per_s": keep * replicates * agents * (hours - 1) / t_abm_screened,
-        "flagged_for_abm_fallback": int(flagged.sum()),
-        "surrogate_peak_rel_err_median": float(np.median(peak_err)),
-        "surrogate_peak_within_5pct": float(np.mean(peak_err <= 0.05)),
-        "screened_best_param_err": float(unit_distance(cand[best][pick], hidden)[0]),
+        "abm_random_s": t_abm_random, "abm_run_s": t_abm_screened / (budget * replicates),
+        "abm_agent_hours_per_s": budget * replicates * agents * (hours - 1) / t_abm_screened,
+        "kept_members_disagree": int(sc["kept_flagged"].sum()),
+        "fallback_uncertain_rank": sc["uncertain"], "fallback_eligible": sc["fallback_eligible"],
+        "fallback_rerun_by_abm": int(len(sc["fallback"])),
+        "pick_from_fallback": bool(pick >= n_kept),
+        "fallback_best_curve_mse": float(err_s[n_kept:].min()) if budget > n_kept else None,
+        "surrogate_peak_rel_err_median": float(np.median(peak_err[:n_kept])),
+        "surrogate_peak_within_5pct": float(np.mean(peak_err[:n_kept] <= 0.05)),
+        "surrogate_peak_rel_err_median_fallback": float(np.median(peak_err[n_kept:])) if budget > n_kept else None,
+        "screened_best_param_err": float(unit_distance(cand[rerun][pick], hidden)[0]),
+        "screened_top8_param_err_mean": float(unit_distance(cand[rerun][top], hidden).mean()),
         "screened_best_curve_mse": float(err_s[pick]),
         "screened_best_peak_rel_err_vs_target": float(relative_peak_error(mean_s[pick:pick + 1], target[None], days)[0]),
-        "random_best_param_err": float(unit_distance(cand[rand_idx][pick_r], hidden)[0]),
-        "random_best_curve_mse": float(err_r[pick_r]),
-        "random_best_peak_rel_err_vs_target": float(relative_peak_error(mean_r[pick_r:pick_r + 1], target[None],
-                                                                         days)[0]),
+        "abm_only_best_param_err": float(unit_distance(cand[rand_idx][pick_r], hidden)[0]),
+        "abm_only_top8_param_err_mean": float(unit_distance(cand[rand_idx][top_r], hidden).mean()),
+        "abm_only_best_curve_mse": float(err_r[pick_r]),
+        "abm_only_best_peak_rel_err_vs_target": float(relative_peak_error(mean_r[pick_r:pick_r + 1], target[None],
+                                                                           days)[0]),
         # candidates whose ABM replicate-mean peak lies within 5 % of the target's, by stage
         "screened_within_5pct_of_target_peak": int((relative_peak_error(mean_s, target[None], days) <= 0.05).sum()),
-        "random_within_5pct_of_target_peak": int((relative_peak_error(mean_r, target[None], days) <= 0.05).sum()),
-        "abm_only_sweep_s_estimated": abm_only_s, "screened_sweep_s": screened_s,
+        "abm_only_within_5pct_of_target_peak": int((relative_peak_error(mean_r, target[None], days) <= 0.05).sum()),
+        "abm_only_sample_runs": budget * replicates,
+        "abm_only_sweep_s_measured_sample": t_abm_random,
+        "abm_only_sweep_s_extrapolated": abm_only_s, "screened_sweep_s": screened_s,
         "sweep_speedup": abm_only_s / screened_s,
     }

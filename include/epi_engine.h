@@ -142,7 +142,7 @@ typedef struct {
     int32_t area_x0, area_y0, area_x1, area_y1; /* current_area rectangle (inclusive) */
 } epi_agent_record;
 
-/* Area rectangle (inclusive corners), engine/src/geography/area.rs:121-126. */
+/* Area rectangle (inclusive corners), engine/src/geography/area.rs:30-35. */
 typedef struct { int32_t x0, y0, x1, y1; } epi_area;
 
 /* Grid layout, engine/src/geography/grid.rs:36-50 (houses/offices as counts + origin). */
@@ -380,8 +380,8 @@ int epi_ensemble_hour_bytes(const epi_ensemble* e, uint32_t hour, double* bytes)
 /* No counterpart in the reference.  One simulated hour (the work of epi_engine_simulate) on
  * device arrays that the caller owns, for callers that cannot allocate device memory: a host
  * runtime whose device memory comes from its own fixed pool or arena and may not grow behind
- * its back, code recording a CUDA graph (cudaMalloc may not be called while a stream is being
- * captured), or a real-time loop that must not enter the driver's allocator.  This entry
+ * its back, or a real-time loop that must not enter the driver's allocator (cudaMalloc can
+ * block on a device-wide synchronisation and take milliseconds).  This entry
  * point calls no cudaMalloc, cudaFree or allocating library routine; its scratch (parameter
  * block, per-agent proposal buffer, (G+1)^2 claim plane) is one fixed 48 MiB device array
  * inside the library, which every GPU that loads the library holds until the process exits.
@@ -400,6 +400,7 @@ int epi_ensemble_hour_bytes(const epi_ensemble* e, uint32_t hour, double* bytes)
  *                     (13-15), infection day (16-31); word 1 = at_hour.  8-byte aligned.
  *   home[n], work[n]  start corners of the 2x2 house / 10x10 office, packed like pos (read only)
  *   work_start_at[n]  hospital staff schedule
+ * pos, home, work, work_start_at and counts must be 4-byte aligned.
  *   plane[(G+3)^2+16] one byte per cell with a one-cell border: cell (x, y) at
  *                     (y+1)*(G+3) + x+1; 0 vacant, 1 occupied, 2/3 infectious at the regular /
  *                     high rate; border and slack bytes zero.  4-byte aligned.

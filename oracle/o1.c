@@ -174,7 +174,7 @@ static int build_world(o1_sim* s) {
     if (n_houses == 0 || n_offices == 0) return EPI_ERR_CONFIG;
     if ((n + n_houses - 1) / n_houses > 4u) return EPI_ERR_CAPACITY; /* grid.rs:140-142 */
     /* transport_area.random_points(ceil(N (pt+0.1)(w+0.1))): only its length matters to the
-     * tick (transport_location is never read by the standalone routine). area.rs:155-165 */
+     * tick (transport_location is never read by the standalone routine). area.rs:64-74 */
     double want = (double)n * (p->public_transport_percentage + 0.1) * (p->working_percentage + 0.1);
     uint64_t n_pt = (uint64_t)ceil(want);
     uint64_t nx = (uint64_t)ceilf(sqrtf((float)n_pt));
@@ -225,7 +225,7 @@ static int build_world(o1_sim* s) {
         free(idx);
     }
     /* start points: house h holds agents h, h+H, h+2H, ... in index order and takes
-     * home.random_points(k) (area.rs:155-165): one agent -> a random cell; k >= 2 ->
+     * home.random_points(k) (area.rs:64-74): one agent -> a random cell; k >= 2 ->
      * choose_multiple of 2 out of 2 values keeps both in order, so the x-major product. */
     for (uint32_t i = 0; i < n; ++i) {
         uint32_t h = i % n_houses, rank = i / n_houses;
@@ -401,7 +401,7 @@ void o1_geography_increase_hospital_size(epi_geography* g, uint32_t grid_size) {
 }
 void o1_philox(const uint32_t ctr[4], const uint32_t key[2], uint32_t out[4]) { orc_philox4x32_10(ctr, key, out); }
 void o1_philox2x32(const uint32_t ctr[2], uint32_t key, uint32_t out[2]) { orc_philox2x32_10(ctr, key, out); }
-/* Area::get_neighbors_of, area.rs:147-149 */
+/* Area::get_neighbors_of, area.rs:56-58 */
 void o1_area_neighbors(int32_t x0, int32_t y0, int32_t x1, int32_t y1, int32_t px, int32_t py, int32_t* out, uint32_t* n) {
     area a = mk_area(x0, y0, x1, y1);
     *n = 0;
@@ -410,7 +410,7 @@ void o1_area_neighbors(int32_t x0, int32_t y0, int32_t x1, int32_t y1, int32_t p
         if (contains(a, q)) { out[2 * *n] = q.x; out[2 * *n + 1] = q.y; ++*n; }
     }
 }
-/* Area::iter, area.rs:210-237: row-major cells */
+/* Area::iter, area.rs:60-62, 131-148: row-major cells */
 uint32_t o1_area_cells(int32_t x0, int32_t y0, int32_t x1, int32_t y1, int32_t* out, uint32_t cap) {
     uint32_t n = 0;
     for (int32_t y = y0; y <= y1; ++y)
@@ -420,7 +420,7 @@ uint32_t o1_area_cells(int32_t x0, int32_t y0, int32_t x1, int32_t y1, int32_t* 
         }
     return n;
 }
-/* area_factory, area.rs:186-208 */
+/* area_factory, area.rs:95-117 */
 uint32_t o1_area_factory(int32_t sx, int32_t sy, int32_t ex, int32_t ey, uint32_t size, int32_t* out, uint32_t cap) {
     int32_t fx = (ex - sx + 1) / (int32_t)size, fy = (ey - sy + 1) / (int32_t)size;
     uint32_t n = 0;

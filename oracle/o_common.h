@@ -37,7 +37,7 @@
 #define WB_HOUR 0xFFFFFFFFu
 
 typedef struct { int32_t x, y; } pt;
-typedef struct { pt s, e; } area; /* inclusive corners, engine/src/geography/area.rs:121-126 */
+typedef struct { pt s, e; } area; /* inclusive corners, engine/src/geography/area.rs:30-35 */
 
 /* engine/src/citizen/mod.rs:48-63 (id = creation index) */
 typedef struct {
@@ -84,17 +84,17 @@ static inline area mk_area(int32_t x0, int32_t y0, int32_t x1, int32_t y1) {
     area a; a.s.x = x0; a.s.y = y0; a.e.x = x1; a.e.y = y1; return a;
 }
 
-/* Area::contains, engine/src/geography/area.rs:174-179 */
+/* Area::contains, engine/src/geography/area.rs:83-88 */
 static inline int contains(area a, pt p) {
     return a.s.x <= p.x && a.e.x >= p.x && a.s.y <= p.y && a.e.y >= p.y;
 }
 
-/* Area PartialEq compares the offsets only, area.rs:129-133 */
+/* Area PartialEq compares the offsets only, area.rs:37-43 */
 static inline int area_eq(area a, area b) {
     return a.s.x == b.s.x && a.s.y == b.s.y && a.e.x == b.e.x && a.e.y == b.e.y;
 }
 
-/* Area::get_random_point, area.rs:167-172 (x drawn first, then y) */
+/* Area::get_random_point, area.rs:76-81 (x drawn first, then y) */
 static inline pt random_point(area a, uint32_t ux, uint32_t uy) {
     pt r; r.x = rng_range(ux, a.s.x, a.e.x); r.y = rng_range(uy, a.s.y, a.e.y); return r;
 }
@@ -115,7 +115,7 @@ static inline double transmission_rate(const epi_params* p, uint32_t day) {
 }
 
 static inline int is_infected(const citizen* c) { return c->state >= EPI_I_PRE && c->state <= EPI_I_SEVERE; }
-/* DiseaseStateMachine::is_symptomatic, disease_state_machine.rs:342-344 */
+/* DiseaseStateMachine::is_symptomatic, disease_state_machine.rs:96-98 */
 static inline int is_symptomatic(const citizen* c) { return c->state == EPI_I_MILD || c->state == EPI_I_SEVERE; }
 /* Citizen::can_move, citizen/mod.rs:452-454 */
 static inline int can_move(const citizen* c) {
@@ -227,7 +227,7 @@ static inline void o_define_geography(o_world* w) {
     w->transport = mk_area(home_width, 0, transport_end - 1, G);
     w->work_area = mk_area(transport_end, 0, work_end - 1, G);
     w->hospital = mk_area(work_end, 0, hospital_end - 1, G);
-    /* area_factory, area.rs:186-208 */
+    /* area_factory, area.rs:95-117 */
     w->hfx = (uint32_t)((w->housing.e.x - w->housing.s.x + 1) / 2);
     w->hfy = (uint32_t)((w->housing.e.y - w->housing.s.y + 1) / 2);
     w->ofx = (uint32_t)((w->work_area.e.x - w->work_area.s.x + 1) / 10);

@@ -158,7 +158,7 @@ static pt hospitalize(const o_world* w, const SNAP_T* m, citizen* c, pt cell, dr
     if (c->hospitalized || c->state != EPI_I_SEVERE) return nc;
     uint32_t dday = (uint32_t)((int32_t)c->day + c->immunity);
     if (!(transmission_rate(&w->p, dday) >= w->p.high_transmission_rate)) return nc;
-    /* hospital_area.iter().find(vacant): AreaIterator order, y outer / x inner (area.rs:221-237) */
+    /* hospital_area.iter().find(vacant): AreaIterator order, y outer / x inner (area.rs:131-148) */
     for (int32_t y = w->hospital.s.y; y <= w->hospital.e.y; ++y) {
         for (int32_t x = w->hospital.s.x; x <= w->hospital.e.x; ++x) {
             pt q; q.x = x; q.y = y;
@@ -188,7 +188,7 @@ static pt deceased(const o_world* w, const SNAP_T* m, citizen* c, pt cell, draws
 static pt routine(const o_world* w, const SNAP_T* m, citizen* c, pt cell, uint32_t hour, draws* d) {
     uint32_t hod = hour % 24u;
     if (hod == 0) {
-        if (is_infected(c)) c->day += 1; /* increment_infection_day, state.rs:241-245 */
+        if (is_infected(c)) c->day += 1; /* increment_infection_day, disease_state_machine.rs:104-106, state.rs:69-73 */
         return hospitalize(w, m, c, cell, d);
     }
     if (hod >= 1 && hod <= 6) {

@@ -7,14 +7,21 @@ resolve in that order -- with its own random stream.  Over many seeds, the epide
 of the engine semantics (lowest index wins; O1 on the CPU, the CUDA engine on the GPU) must
 match O2's: peak height, peak day and final attack rate agree within a 4-sigma band of the
 difference of means, and a two-sample Kolmogorov-Smirnov test does not reject (p > 1e-3).
+
+Two workloads: config 1 of the benchmarks (small_pox_10k_250.json: 10,000 agents on a 250
+grid, small pox, 5 exposed, 2,400 hours), against 200 O2 runs that
+tests/golden/make_distribution_goldens.py committed; and a faster, denser disease on a 2,000
+agent world with a lockdown, whose 200 O2 runs are made live.
 """
+import importlib.util
 import json
 import multiprocessing as mp
+import os
 
 import numpy as np
 import pytest
 
-from helpers import make_config
+from helpers import GOLDEN, make_config
 
 SMALL_POX_FAST = {
     "regular_transmission_start_day": 2, "high_transmission_start_day": 5, "last_day": 9,
@@ -102,4 +109,38 @@ def test_engine_matches_reference_order_semantics_in_distribution(gpu, oracle_mo
         eng.close()
     a = np.array(a)
     assert a[:, 2].mean() > 0.2
+    _compare(a, b)
+
+
+def _golden_module():
+    spec = importlib.util.spec_from_file_location("make_distribution_goldens",
+                                                  os.path.join(GOLDEN, "make_distribution_goldens.py"))
+    mod = importlib.util.module_from_spec(spec)
+    spec.loader.exec_module(mod)
+    return mod
+
+
+def test_config1_o2_sample_is_complete():
+    with open(os.path.join(GOLDEN, "o2_small_pox_10k_250_200.json")) as f:
+        g = json.load(f)
+    runs = np.array(g["runs"], dtype=np.float64)
+    assert runs.shape == (200, 4)
+    assert (runs[:, 0] >= 5).all() and (runs[:, 2] > 0).all() and (runs[:, 3] <= 2399).all()
+
+
+@pytest.mark.gpu
+def test_engine_matches_reference_order_semantics_config1(gpu):
+    """Config 1 (small pox, 10,000 agents, 250 grid, 2,400 h): the GPU engine over 200 seeds
+    (1000..1199, one 200-replicate ensemble; each replicate equals a lone engine bit for bit)
+    against the committed O2 sample (seeds 5000..5199): peak of active cases, its day and the
+    final attack rate."""
+    pytest.importorskip("scipy")
+    from epirust_gb300 import Config, Ensemble
+
+    gen = _golden_module()
+    with open(os.path.join(GOLDEN, "o2_small_pox_10k_250_200.json")) as f:
+        b = np.array(json.load(f)["runs"], dtype=np.float64)[:, :3]
+    ens = Ensemble([Config(json.dumps(gen.config_with_seed(1000 + s))).params for s in range(200)])
+    a = np.array([gen.summary(r, 10_000)[:3] for r in ens.run()], dtype=np.float64)
+    ens.close()
     _compare(a, b)

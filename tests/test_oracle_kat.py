@@ -66,22 +66,22 @@ def test_small_pox_rates(oracle_mod):
 
 
 def test_area_neighbors_and_moore_order(oracle_mod):
-    # engine/src/geography/area.rs:318-325
+    # engine/src/geography/area.rs:227-234
     nb = oracle_mod.area_neighbors((0, 0, 5, 5), (4, 5))
     assert len(nb) == 5 and (4, 4) in nb and (4, 6) not in nb
-    # engine/src/geography/point.rs:442-459 (offset order)
+    # engine/src/geography/point.rs:84-101 (offset order)
     assert oracle_mod.area_neighbors((-10, -10, 10, 10), (1, 1)) == \
         [(0, 0), (1, 0), (2, 0), (0, 1), (2, 1), (0, 2), (1, 2), (2, 2)]
 
 
 def test_area_iteration_order(oracle_mod):
-    # engine/src/geography/area.rs:255-277
+    # engine/src/geography/area.rs:164-186
     assert oracle_mod.area_cells((0, 0, 2, 2)) == [(0, 0), (1, 0), (2, 0), (0, 1), (1, 1), (2, 1), (0, 2), (1, 2), (2, 2)]
     assert oracle_mod.area_cells((1, 1, 2, 2)) == [(1, 1), (2, 1), (1, 2), (2, 2)]
 
 
 def test_area_factory(oracle_mod):
-    # engine/src/geography/area.rs:289-316
+    # engine/src/geography/area.rs:198-225
     b = oracle_mod.area_factory((10, 0), (21, 10), 3)
     assert len(b) == 12
     assert b[0] == (10, 0, 12, 2)
@@ -96,7 +96,7 @@ def test_starting_infection_split(oracle_mod):
     st = recs["state"]
     assert (st == I_ASYM).sum() == 2 and (st == I_MILD).sum() == 3
     assert (st == I_SEVERE).sum() == 4 and (st == E).sum() == 5
-    # starting infected agents are on day 1, exposed at hour 0 (disease_state_machine.rs:354-367)
+    # starting infected agents are on day 1, exposed at hour 0 (citizen_factory.rs:122-133, disease_state_machine.rs:109-121)
     assert set(recs["infection_day"][(st >= I_PRE) & (st <= I_SEVERE)]) == {1}
     assert set(recs["at_hour"][st == E]) == {0}
 

@@ -221,6 +221,20 @@ def test_surrogate_gain_over_method_without_it(gpu):
     err = ((abm - target) ** 2).mean(axis=1)
     assert err[:16].min() <= err[16:].min()
     assert np.median(err[:16]) < np.median(err[16:])
+
+    # the ABM fallback: candidates outside the kept set that some member would keep and whose
+    # members' peaks disagree by more than 5 % are handed to the ABM, most promising first
+    from epirust_gb300.surrogate import member_peak_spread, screen_with_fallback
+
+    sc = screen_with_fallback(net, cand, target, keep=16, days=days, peak_tolerance=0.05, max_fallback=64)
+    assert np.array_equal(sc["kept"], best)
+    fb = sc["fallback"]
+    assert len(fb) > 0 and not set(fb.tolist()) & set(best.tolist())
+    assert len(fb) == min(64, sc["fallback_eligible"]) and sc["fallback_eligible"] <= sc["uncertain"]
+    members = net.score_members(cand, target)
+    cut = members.mean(axis=0)[best].max()
+    assert (members[:, fb].min(axis=0) <= cut).all()
+    assert (member_peak_spread(net, cand[fb], days) > 0.05).all()
     net.close()
 
 

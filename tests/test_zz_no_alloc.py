@@ -1,10 +1,13 @@
 """epi_tick_hour_noalloc: one hour on caller-owned device arrays, with no device allocation.
 
-Callers whose device memory comes from their own fixed pool, that record CUDA graphs, or
-that must stay out of the driver's allocator on their hot path cannot let the library call
-cudaMalloc.  This test packs a mid-epidemic world into device arrays it owns (allocated here
-by torch), runs two hours in a row through the no-allocation entry point of the C ABI, and
-checks the counts and every agent word against the engine's regular entry point
+Callers whose device memory comes from their own fixed pool or arena, or that must stay out
+of the driver's allocator on their hot path, cannot let the library call cudaMalloc.  These
+tests pack a mid-epidemic world into device arrays they own (allocated here by torch), run
+it hour after hour through the no-allocation entry point of the C ABI -- a whole day and
+across the day boundary, so every hour class runs (the hospital scan of hour 0, the sleep
+hours, the travel, work, noon, home and walking hours, the deaths and recoveries of hour
+23), once with the original hospital and once after BuildNewHospital grew it -- and check
+the counts and every agent word after every hour against the engine's regular entry point
 (epi_engine_simulate) on the same world.  Integer state: the results must be identical.
 
 The file is named to be collected last, so that a run stopping at the first failure has
@@ -97,15 +100,14 @@ def _unpack(pos, state, wsa, like, geo, grown):
     return out
 
 
-def test_noalloc_hours_match_engine(gpu):
+def _noalloc_against_engine(cfg, warm_hours, hours, grow_hospital):
+    """Run `hours` through epi_tick_hour_noalloc and through epi_engine_simulate from the same
+    world (the regular engine after `warm_hours`); compare counts and agents every hour."""
     import torch
 
     from epirust_gb300 import Config, Epidemiology, lib
     from epirust_gb300._lib import EpiGeography
 
-    cfg = make_config(n=4000, grid=120, seed=21, disease=COVID_FAST, starting=(5, 5, 5, 30),
-                      interventions=[{"Lockdown": {"at_number_of_infections": 10 ** 6,
-                                                   "essential_workers_population": 0.2}}])
     config = Config(json.dumps(cfg))
     p = config.params
     L = lib()
@@ -114,17 +116,15 @@ def test_noalloc_hours_match_engine(gpu):
     assert L.epi_resize_hospital(C.byref(geo), p.number_of_agents, 0.002, p.hospital_beds_percentage) == 0
     grown = (geo.hospital.x0, geo.hospital.y0, p.grid_size, p.grid_size)
 
-    # a mid-epidemic world from the regular engine: 4 days and the night of the 5th
     base = Epidemiology(config)
-    base.simulate_hours(1, 24 * 4 + 6)
+    base.simulate_hours(1, warm_hours)
     world = base.snapshot()
     base.close()
-    hours = (24 * 4 + 7, 24 * 4 + 8)
 
     ref = Epidemiology(config, records=world)
-    ref_counts = [ref.simulate(h) for h in hours]
-    ref_agents = ref.snapshot()
-    ref.close()
+    if grow_hospital:
+        ref.increase_hospital_size()
+        assert ref.geography().hospital.x1 == p.grid_size
 
     dev = torch.device("cuda")
     # u32 words travel as int32 tensors (same bits)
@@ -133,19 +133,49 @@ def test_noalloc_hours_match_engine(gpu):
     pos, state, home, work, wsa, plane = arrays
     counts = torch.zeros(8, dtype=torch.int32, device=dev)
     stream = torch.cuda.current_stream().cuda_stream
-    for h, want in zip(hours, ref_counts):
-        rc = L.epi_tick_hour_noalloc(C.byref(p), h, 0, pos.data_ptr(), state.data_ptr(), home.data_ptr(),
-                                     work.data_ptr(), wsa.data_ptr(), plane.data_ptr(), counts.data_ptr(), stream)
+    seen_states = set()
+    for h in hours:
+        want = ref.simulate(h)
+        rc = L.epi_tick_hour_noalloc(C.byref(p), h, 1 if grow_hospital else 0, pos.data_ptr(), state.data_ptr(),
+                                     home.data_ptr(), work.data_ptr(), wsa.data_ptr(), plane.data_ptr(),
+                                     counts.data_ptr(), stream)
         assert rc == 0, L.epi_engine_last_error(None)
         got = counts.cpu().numpy().astype(np.int64)[:6]
         assert list(got) == [want.susceptible, want.exposed, want.infected, want.hospitalized, want.recovered,
                              want.deceased], h
-    out = _unpack(pos.cpu().numpy().view(np.uint32), state.cpu().numpy().view(np.uint32),
-                  wsa.cpu().numpy().view(np.uint32), world, geo, grown)
-    for name in ref_agents.dtype.names:
-        assert (out[name] == ref_agents[name]).all(), name
-    # the plane the caller owns reflects the new positions: one occupied byte per agent
-    assert int((plane.cpu().numpy() != 0).sum()) == len(world)
+        ref_agents = ref.snapshot()
+        out = _unpack(pos.cpu().numpy().view(np.uint32), state.cpu().numpy().view(np.uint32),
+                      wsa.cpu().numpy().view(np.uint32), world, geo, grown)
+        for name in ref_agents.dtype.names:
+            assert (out[name] == ref_agents[name]).all(), (h, name)
+        seen_states.update(int(v) for v in np.unique(ref_agents["state"]))
+        # the plane the caller owns reflects the new positions: one occupied byte per agent
+        assert int((plane.cpu().numpy() != 0).sum()) == len(world), h
+    ref.close()
+    return ref_agents, seen_states
+
+
+# hour of day 6 of day 7 through hour of day 1 of day 8: every hour class, in order, while
+# agents are exposed, severe, hospitalised, recovering and dying
+DAY_HOURS = tuple(range(24 * 7 + 6, 24 * 8 + 2))
+
+
+def test_noalloc_hours_match_engine(gpu):
+    """A whole day and the next day boundary, original hospital."""
+    cfg = make_config(n=4000, grid=120, seed=21, disease=COVID_FAST, starting=(5, 5, 5, 30),
+                      interventions=[{"Lockdown": {"at_number_of_infections": 10 ** 6,
+                                                   "essential_workers_population": 0.2}}])
+    agents, states = _noalloc_against_engine(cfg, DAY_HOURS[0] - 1, DAY_HOURS, grow_hospital=False)
+    assert {1, 5, 6, 7}.issubset(states)         # exposed, severe, recovered and dead agents took part
+    assert (agents["flags"] & 1).any()            # and someone is in hospital
+
+
+def test_noalloc_hours_match_engine_grown_hospital(gpu):
+    """The same day on a world whose hospital BuildNewHospital has grown (staff and patients
+    compare their area with the grown rectangle)."""
+    cfg = make_config(n=4000, grid=120, seed=22, disease=COVID_FAST, starting=(5, 5, 10, 30), beds=0.001)
+    agents, states = _noalloc_against_engine(cfg, DAY_HOURS[0] - 1, DAY_HOURS, grow_hospital=True)
+    assert (agents["flags"] & 1).any()
 
 
 def test_noalloc_rejects_worlds_beyond_its_scratch(gpu):
@@ -164,3 +194,10 @@ def test_noalloc_rejects_worlds_beyond_its_scratch(gpu):
     rc = lib().epi_tick_hour_noalloc(C.byref(small), 7, 0, ptr, ptr, ptr, ptr, ptr, ptr + 1, ptr, None)
     assert rc == EPI_ERR_ARG
     assert b"4-byte aligned" in lib().epi_engine_last_error(None)
+    # so are per-agent arrays and counts that are not 4-byte aligned
+    for k in (0, 2, 3, 4, 6):
+        args = [ptr] * 7
+        args[k] = ptr + 2
+        rc = lib().epi_tick_hour_noalloc(C.byref(small), 7, 0, *args, None)
+        assert rc == EPI_ERR_ARG, k
+        assert b"4-byte aligned" in lib().epi_engine_last_error(None)
