@@ -199,15 +199,75 @@ __global__ void __launch_bounds__(kThreads) k_sleep(const DevParams* __restrict_
     flush_rep(br, sh, row_ptr(ha, hr.row));
 }
 
-// One hour of per-agent rules (hour of day 0, 7..22 or 23), specialised per hour class HC.
-// The body is shared by two kernels that differ only in their launch bounds: k_decide for a
-// single world (registers left to the compiler: 55 for the movement classes) and
-// k_decide_ens for ensembles (at least kEnsembleMinBlocks resident blocks: 48 registers),
-// whose per-chunk replicate switches favour occupancy; each was measured faster on its own
-// workload.
+// The rules of one agent for the hour (slot valid): proposal, claim, infection update, state
+// and target words.  Returns the agent's counts bin.
+template <int HC>
+__device__ __forceinline__ uint32_t decide_agent(const DevParams& P, const PlaneView& pl, uint32_t* __restrict__ rclaim,
+                                                 uint32_t* __restrict__ wsa, uint2* __restrict__ st,
+                                                 uint32_t* __restrict__ tgt, uint32_t* __restrict__ lost, uint32_t slot,
+                                                 uint32_t i, uint32_t s, uint32_t at, uint32_t p, uint32_t hm, uint32_t wk,
+                                                 uint32_t hour, uint32_t hod, uint32_t hosp_first, int* err) {
+    const uint32_t s0 = s, at0 = at;
+    const Cell cell{unpack_x(p), unpack_y(p)};
+    Draws dr{i, hour, P.key0, P.key1, P.move_key};
+    Cell nc;
+    bool infect = false;
+    if (HC == kHcStart) {
+        nc = routine_start(P, pl, s, hm, cell, hosp_first, dr);
+    } else if (HC == kHcEnd) {
+        nc = routine_end(P, pl, s, hm, cell, dr);
+    } else {
+        const bool staff = st_ws(s) == EPI_WS_HOSPITAL_STAFF;
+        uint32_t w0 = staff ? wsa[slot] : 0u, w = w0;
+        nc = perform_movements<HC>(P, pl, s, w, hm, wk, cell, hod, hour, dr, infect);
+        if (staff && w != w0) wsa[slot] = w;
+    }
+    bool moving = nc.x != cell.x || nc.y != cell.y;
+    if (moving && ((uint32_t)nc.x > (uint32_t)P.G || (uint32_t)nc.y > (uint32_t)P.G)) {
+        atomicOr(err, 4);  // unreachable for validated worlds; never write outside the plane
+        moving = false;
+        nc = cell;
+    }
+    // The claim goes out before the infection update so that its round trip overlaps it.
+    const uint32_t key = claim_key(hour, i);
+    const uint32_t old = moving ? atomicMin(&rclaim[(size_t)nc.y * P.W + nc.x], key) : kNoClaim;
+    if (infect) infection_dynamics(P, pl, s, at, hm, wk, nc, hour, dr);
+    if (moving) {
+        // The claim that atomicMin finds names an agent this one competes with: of the two
+        // the higher index loses.  Every claimant but the cell's lowest is named so, by
+        // itself or by the claimant that displaced it, so the loss marks settle the cell
+        // without a second read of the claim plane.
+        if (lost && old != kNoClaim && (old >> kClaimAgentBits) == (key >> kClaimAgentBits)) {
+            const uint32_t j = old & kMaxAgentsPerWorld;
+            if (j < i) {
+                moving = false;
+                nc = cell;
+            } else {
+                lost[P.agent_off + j] = hour;
+            }
+        }
+    }
+    // the plane byte changes when the agent moves or its class changes (s == s0 keeps it)
+    uint32_t t = kNoAction;
+    if (moving || s != s0) {
+        const uint32_t cls0 = cell_class(P, s0), cls = s == s0 ? cls0 : cell_class(P, s);
+        if (moving || cls != cls0) t = encode_target(nc, cls, cls0);
+    }
+    tgt[slot] = t;
+    if (s != s0 || at != at0) st[slot] = make_uint2(s, at);
+    return count_bin(s);
+}
+
+// One hour of per-agent rules (hour of day 0, 7..22 or 23), specialised per hour class HC,
+// over one world (ENS false: slot = agent, the parameters staged once) or the chunks of many
+// replicates (ENS true: chunk_rep names each chunk's replicate).  The body is shared by two
+// kernels that differ in their launch bounds: k_decide for a single world (registers left to
+// the compiler) and k_decide_ens for ensembles (at least kEnsembleMinBlocks resident blocks:
+// 48 registers), whose per-chunk replicate switches favour occupancy; each was measured
+// faster on its own workload.
 constexpr int kEnsembleMinBlocks = 5;
 
-template <int HC>
+template <int HC, bool ENS>
 __device__ __forceinline__ void decide_body(const DevParams* __restrict__ Pall, const uint32_t* __restrict__ chunk_rep,
                                             uint32_t n_chunks, const uint32_t* __restrict__ pos, uint2* __restrict__ st,
                                             const uint32_t* __restrict__ home, const uint32_t* __restrict__ work,
@@ -224,11 +284,45 @@ __device__ __forceinline__ void decide_body(const DevParams* __restrict__ Pall, 
     const uint32_t hod = hour % 24u;
     BlockRep br;
     uint32_t hosp_first = kNoAction;
-    bool hosp_known = false, ended = false;
-    const uint32_t grp = chunk_rep ? kEnsembleChunkGroup : kWorldChunkGroup;  // chunks per stride step
+    bool hosp_known = false;
+    if (!ENS) {
+        if (blockIdx.x >= n_chunks) return;  // block-uniform: nothing to do or count
+        switch_rep(br, 0u, Pall, sP, sh, row_ptr(ha, hr.row));
+        if (P.active && !run_ended(prev_ptr(ha, hr.row), 0u)) {
+            const PlaneView pl{plane + P.plane_off, P.G, P.WP, err, danger ? danger + P.plane_off : nullptr};
+            uint32_t* rclaim = claim + P.claim_off;
+            const uint32_t n = P.n;
+            for (uint32_t c = blockIdx.x; c < n_chunks; c += gridDim.x) {
+                const uint32_t slot = c * kChunk + threadIdx.x;  // = agent index (a lone world starts at slot 0)
+                const bool valid = slot < n;
+                uint32_t s = 0, at = 0, p = 0;
+                if (valid) {
+                    const uint2 sv = st[slot];
+                    s = sv.x;
+                    at = sv.y;
+                    p = pos[slot];
+                }
+                if (HC == kHcStart) {
+                    const bool need = valid && wants_hospital(P, infected(s) ? with_day(s, st_day(s) + 1u) : s);
+                    if (__syncthreads_or(need) && !hosp_known) {
+                        hosp_first = block_first_vacant(P, pl);
+                        hosp_known = true;
+                    }
+                }
+                const uint32_t bin = valid ? decide_agent<HC>(P, pl, rclaim, wsa, st, tgt, lost, slot, slot, s, at, p,
+                                                              home[slot], work[slot], hour, hod, hosp_first, err)
+                                           : 0u;
+                count_into(sh, valid, bin);
+            }
+        }
+        flush_rep(br, sh, row_ptr(ha, hr.row));
+        return;
+    }
+    bool ended = false;
+    const uint32_t grp = kEnsembleChunkGroup;  // chunks per stride step
     for (uint32_t c = blockIdx.x * grp, k = 0; c < n_chunks;
          c = (++k < grp) ? c + 1u : c + (gridDim.x - 1u) * grp + 1u, k = (k < grp) ? k : 0u) {
-        const uint32_t r = chunk_rep ? chunk_rep[c] : 0u;
+        const uint32_t r = chunk_rep[c];
         if (r != br.r) {
             switch_rep(br, r, Pall, sP, sh, row_ptr(ha, hr.row));
             hosp_known = false;
@@ -254,59 +348,9 @@ __device__ __forceinline__ void decide_body(const DevParams* __restrict__ Pall, 
                 hosp_known = true;
             }
         }
-        uint32_t bin = 0;
-        if (valid) {
-            const uint32_t s0 = s, at0 = at;
-            const uint32_t hm = home[slot], wk = work[slot];
-            const Cell cell{unpack_x(p), unpack_y(p)};
-            Draws dr{i, hour, P.key0, P.key1, P.move_key};
-            Cell nc;
-            bool infect = false;
-            if (HC == kHcStart) {
-                nc = routine_start(P, pl, s, hm, cell, hosp_first, dr);
-            } else if (HC == kHcEnd) {
-                nc = routine_end(P, pl, s, hm, cell, dr);
-            } else {
-                const bool staff = st_ws(s) == EPI_WS_HOSPITAL_STAFF;
-                uint32_t w0 = staff ? wsa[slot] : 0u, w = w0;
-                nc = perform_movements<HC>(P, pl, s, w, hm, wk, cell, hod, hour, dr, infect);
-                if (staff && w != w0) wsa[slot] = w;
-            }
-            bool moving = nc.x != cell.x || nc.y != cell.y;
-            if (moving && ((uint32_t)nc.x > (uint32_t)P.G || (uint32_t)nc.y > (uint32_t)P.G)) {
-                atomicOr(err, 4);  // unreachable for validated worlds; never write outside the plane
-                moving = false;
-                nc = cell;
-            }
-            // The claim goes out before the infection update so that its round trip overlaps it.
-            const uint32_t key = claim_key(hour, i);
-            const uint32_t old = moving ? atomicMin(&rclaim[(size_t)nc.y * P.W + nc.x], key) : kNoClaim;
-            if (infect) infection_dynamics(P, pl, s, at, hm, wk, nc, hour, dr);
-            if (moving) {
-                // The claim that atomicMin finds names an agent this one competes with: of
-                // the two the higher index loses.  Every claimant but the cell's lowest is
-                // named so, by itself or by the claimant that displaced it, so the loss
-                // marks settle the cell without a second read of the claim plane.
-                if (lost && old != kNoClaim && (old >> kClaimAgentBits) == (key >> kClaimAgentBits)) {
-                    const uint32_t j = old & kMaxAgentsPerWorld;
-                    if (j < i) {
-                        moving = false;
-                        nc = cell;
-                    } else {
-                        lost[P.agent_off + j] = hour;
-                    }
-                }
-            }
-            // the plane byte changes when the agent moves or its class changes (s == s0 keeps it)
-            uint32_t t = kNoAction;
-            if (moving || s != s0) {
-                const uint32_t cls = cell_class(P, s), cls0 = cell_class(P, s0);
-                if (moving || cls != cls0) t = encode_target(nc, cls, cls0);
-            }
-            tgt[slot] = t;
-            if (s != s0 || at != at0) st[slot] = make_uint2(s, at);
-            bin = count_bin(s);
-        }
+        const uint32_t bin = valid ? decide_agent<HC>(P, pl, rclaim, wsa, st, tgt, lost, slot, i, s, at, p, home[slot],
+                                                      work[slot], hour, hod, hosp_first, err)
+                                   : 0u;
         count_into(sh, valid, bin);
     }
     flush_rep(br, sh, row_ptr(ha, hr.row));
@@ -320,11 +364,11 @@ __device__ __forceinline__ void decide_body(const DevParams* __restrict__ Pall, 
         uint32_t *__restrict__ lost, HourArgs ha, int *err
 template <int HC>
 __global__ void __launch_bounds__(kThreads) k_decide(EPI_DECIDE_PARAMS) {
-    decide_body<HC>(Pall, chunk_rep, n_chunks, pos, st, home, work, wsa, plane, danger, claim, tgt, lost, ha, err);
+    decide_body<HC, false>(Pall, chunk_rep, n_chunks, pos, st, home, work, wsa, plane, danger, claim, tgt, lost, ha, err);
 }
 template <int HC>
 __global__ void __launch_bounds__(kThreads, kEnsembleMinBlocks) k_decide_ens(EPI_DECIDE_PARAMS) {
-    decide_body<HC>(Pall, chunk_rep, n_chunks, pos, st, home, work, wsa, plane, danger, claim, tgt, lost, ha, err);
+    decide_body<HC, true>(Pall, chunk_rep, n_chunks, pos, st, home, work, wsa, plane, danger, claim, tgt, lost, ha, err);
 }
 #undef EPI_DECIDE_PARAMS
 

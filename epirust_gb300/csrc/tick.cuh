@@ -55,20 +55,30 @@ struct PlaneView {
         }
         return __ldg(danger + (size_t)(y + 1) * (size_t)WP + (size_t)(x + 1));
     }
-    // Bytes of (x-1, y), (x, y), (x+1, y) in bits 0-7, 8-15, 16-23.
+    // Bytes of (x-1, y), (x, y), (x+1, y) in bits 0-7, 8-15, 16-23 (bits 24-31: the next
+    // byte of the row, which no caller reads).
     __device__ __forceinline__ uint32_t row3(int32_t x, int32_t y) const {
         const uintptr_t a = (uintptr_t)(cells + (size_t)(y + 1) * (size_t)WP + (size_t)x);
         const uint32_t* w = (const uint32_t*)(a & ~(uintptr_t)3);
         const uint32_t lo = __ldg(w), hi = __ldg(w + 1);
-        return __funnelshift_r(lo, hi, (uint32_t)(a & 3u) * 8u) & 0xFFFFFFu;
+        return __funnelshift_r(lo, hi, (uint32_t)(a & 3u) * 8u);
     }
 };
 
-// Gather the per-byte flag bits (bits 0, 8, 16 of each row) into NeighborIterator order.
-__device__ __forceinline__ uint32_t gather8(uint32_t f0, uint32_t f1, uint32_t f2) {
-    return (f0 & 1u) | ((f0 >> 7) & 2u) | ((f0 >> 14) & 4u) | ((f1 & 1u) << 3) | ((f1 >> 12) & 16u) |
-           ((f2 & 1u) << 5) | ((f2 >> 2) & 64u) | ((f2 >> 9) & 128u);
+// The eight neighbour bytes of a 3x3 block in NeighborIterator order, as two words: bytes of
+// lo = neighbours 0-3 (row 0 bytes 0-2, row 1 byte 0), bytes of hi = neighbours 4-7 (row 1
+// byte 2, row 2 bytes 0-2).  Two byte permutes; byte 3 of a row is never selected.
+struct Nb8 {
+    uint32_t lo, hi;
+};
+__device__ __forceinline__ Nb8 neighbour_bytes(uint32_t r0, uint32_t r1, uint32_t r2) {
+    return Nb8{__byte_perm(r0, r1, 0x4210u), __byte_perm(r1, r2, 0x6542u)};
 }
+// Bit 0 of each byte of f (other bits zero) -> 4 bits, byte k to bit k: the product spreads
+// byte k's bit to bit 24 + k with no carries (the other partial products land on distinct
+// bits below 24 or beyond bit 31).
+__device__ __forceinline__ uint32_t pack4(uint32_t f) { return (f * 0x01020408u) >> 24; }
+__device__ __forceinline__ uint32_t pack8(uint32_t flo, uint32_t fhi) { return pack4(flo) | (pack4(fhi) << 4); }
 
 // The three rows of the 3x3 block around (x, y); a cell outside [0, G]^2 reads as a
 // block of occupied, non-infectious cells (and is reported).
@@ -84,19 +94,23 @@ __device__ __forceinline__ Rows3 rows_around(const PlaneView& pl, int32_t x, int
 }
 
 // Plane bytes are 0..3: occupied <=> bit0|bit1, infectious <=> bit1, high rate <=> bit0&bit1.
+// Masks are 8 bits in NeighborIterator order.
 __device__ __forceinline__ uint32_t occupied_mask(const Rows3& r) {
-    const uint32_t m = 0x010101u;
-    return gather8((r.r0 | (r.r0 >> 1)) & m, (r.r1 | (r.r1 >> 1)) & m, (r.r2 | (r.r2 >> 1)) & m);
+    const Nb8 b = neighbour_bytes(r.r0, r.r1, r.r2);
+    const uint32_t m = 0x01010101u;
+    return pack8((b.lo | (b.lo >> 1)) & m, (b.hi | (b.hi >> 1)) & m);
 }
 // Any infectious byte among the nine (the centre is vacant or the agent's own, never infectious).
 __device__ __forceinline__ bool any_infectious(const Rows3& r) { return ((r.r0 | r.r1 | r.r2) & 0x020202u) != 0u; }
 __device__ __forceinline__ uint32_t infectious_mask(const Rows3& r) {
-    const uint32_t m = 0x010101u;
-    return gather8((r.r0 >> 1) & m, (r.r1 >> 1) & m, (r.r2 >> 1) & m);
+    const Nb8 b = neighbour_bytes(r.r0, r.r1, r.r2);
+    const uint32_t m = 0x01010101u;
+    return pack8((b.lo >> 1) & m, (b.hi >> 1) & m);
 }
 __device__ __forceinline__ uint32_t high_mask(const Rows3& r) {
-    const uint32_t m = 0x010101u;
-    return gather8(r.r0 & (r.r0 >> 1) & m, r.r1 & (r.r1 >> 1) & m, r.r2 & (r.r2 >> 1) & m);
+    const Nb8 b = neighbour_bytes(r.r0, r.r1, r.r2);
+    const uint32_t m = 0x01010101u;
+    return pack8(b.lo & (b.lo >> 1) & m, b.hi & (b.hi >> 1) & m);
 }
 
 // Neighbours of (x, y) inside area a and the grid (Area::get_neighbors_of filtered by
@@ -199,9 +213,13 @@ __device__ __forceinline__ Cell move_agent_from(const PlaneView& pl, uint32_t s,
     if (!can_move(s)) return cell;
     Cell c = cell;
     if (!rect_has(cur, cell.x, cell.y)) c = random_point(cur, dr.m(0), dr.m(1));
-    const uint32_t cand = valid_neighbours(cur, pl.G, c.x, c.y) & ~occupied_mask(rows_around(pl, c.x, c.y));
+    const Rows3 rows = rows_around(pl, c.x, c.y);
+    // The choice word is drawn before the rows are used, so that its Philox rounds run while
+    // the row loads are in flight (it is needed unless every neighbour is taken).
+    const uint32_t u = dr.m(2);
+    const uint32_t cand = valid_neighbours(cur, pl.G, c.x, c.y) & ~occupied_mask(rows);
     if (!cand) return cell;
-    const uint32_t j = uniform_index(dr.m(2), (uint32_t)__popc(cand));
+    const uint32_t j = uniform_index(u, (uint32_t)__popc(cand));
     const int k = nth_set_bit8(cand, j);
     return Cell{c.x + nb_dx(k), c.y + nb_dy(k)};     // vacant by construction: move_agent keeps it
 }
