@@ -24,9 +24,9 @@
 namespace epi {
 
 // Moore offsets in NeighborIterator order (engine/src/geography/point.rs:59), packed as
-// 2-bit (d + 1) fields: k-th neighbour = (x + dx(k), y + dy(k)).
-__device__ __forceinline__ int32_t nb_dx(int k) { return (int32_t)((0x9224u >> (2 * k)) & 3u) - 1; }
-__device__ __forceinline__ int32_t nb_dy(int k) { return (int32_t)((0xA940u >> (2 * k)) & 3u) - 1; }
+// 2-bit (d + 1) fields: k-th neighbour = (x + dx(k), y + dy(k)) with dx(k) + 1 the k-th field
+// of kMooreDx and dy(k) + 1 that of kMooreDy.
+constexpr uint32_t kMooreDx = 0x9224u, kMooreDy = 0xA940u;
 
 struct PlaneView {
     const uint8_t* __restrict__ cells;  // padded plane: cell (x, y) at (y + 1) * WP + (x + 1)
@@ -127,16 +127,24 @@ __device__ __forceinline__ uint32_t valid_neighbours(const Rect& a, int32_t G, i
     return top | (mid << 3) | (bot << 5);
 }
 
-// Position of the j-th set bit (j counted from 0, j < popc(m)) of an 8-bit mask.
-__device__ __forceinline__ int nth_set_bit8(uint32_t m, uint32_t j) {
-    int base = 0;
-    const uint32_t c4 = (uint32_t)__popc(m & 0xFu);
-    if (j >= c4) { j -= c4; m >>= 4; base = 4; }
-    const uint32_t c2 = (uint32_t)__popc(m & 0x3u);
-    if (j >= c2) { j -= c2; m >>= 2; base += 2; }
-    if (j >= (m & 1u)) base += 1;
-    return base;
+// Moore step of the j-th set bit of an 8-bit neighbour mask, as (dx + 1) | (dy + 1) << 2,
+// for every mask and j < popc(mask): one table read instead of the bit search.
+struct StepTable {
+    uint8_t v[256][8];
+};
+constexpr StepTable make_step_table() {
+    StepTable t{};
+    for (int m = 0; m < 256; ++m) {
+        int j = 0;
+        for (int k = 0; k < 8; ++k)
+            if ((m >> k) & 1) {
+                const int dx = (int)((kMooreDx >> (2 * k)) & 3u), dy = (int)((kMooreDy >> (2 * k)) & 3u);
+                t.v[m][j++] = (uint8_t)(dx | (dy << 2));
+            }
+    }
+    return t;
 }
+__device__ const StepTable kStepTable = make_step_table();
 
 // Lazily materialised Philox blocks of one agent-hour: m(0), m(1) the random-point words
 // and m(2) the choice word (Philox2x32 each), d(), d2() the disease blocks (Philox4x32).
@@ -220,8 +228,8 @@ __device__ __forceinline__ Cell move_agent_from(const PlaneView& pl, uint32_t s,
     const uint32_t cand = valid_neighbours(cur, pl.G, c.x, c.y) & ~occupied_mask(rows);
     if (!cand) return cell;
     const uint32_t j = uniform_index(u, (uint32_t)__popc(cand));
-    const int k = nth_set_bit8(cand, j);
-    return Cell{c.x + nb_dx(k), c.y + nb_dy(k)};     // vacant by construction: move_agent keeps it
+    const uint32_t e = __ldg(&kStepTable.v[cand][j]);
+    return Cell{c.x + (int32_t)(e & 3u) - 1, c.y + (int32_t)(e >> 2) - 1};  // vacant by construction: move_agent keeps it
 }
 
 // Citizen::goto_area, citizen/mod.rs:367-395

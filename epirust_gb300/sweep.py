@@ -37,13 +37,15 @@ def grid_for(agents: int, density: float = 0.16) -> int:
 def train_on_abm(runs: int = 4096, held_out: int = 512, agents: int = 100_000, days: int = 100,
                  members: int = 5, steps: int = 3000, seed: int = 4, hidden: int = 512, hidden_layers: int = 3,
                  batch: int = 256, abm_batch: int = 512, per_agents: int = 100_000, curves: np.ndarray | None = None,
-                 noise_runs: int = 128, mean_points: int = 128, mean_replicates: int = 8):
+                 noise_runs: int = 128, mean_points: int = 128, mean_replicates: int = 8, grid: int | None = 790):
     """curves: ABM curves of this design computed before (skips the ABM stage).  noise_runs
     held-out points are simulated again with other seeds to measure the ABM's own peak-height
     spread, the floor of any surrogate's error against single runs.  mean_points held-out
     points are run mean_replicates more times and the network's peak height is judged against
-    the mean of those runs (the ABM ensemble mean, which is what a sweep compares)."""
-    grid = grid_for(agents)
+    the mean of those runs (the ABM ensemble mean, which is what a sweep compares).  grid: the
+    training worlds' grid side (790 for the 100,000-agent runs of the training workload; None
+    for ceil(sqrt(agents / 0.16)))."""
+    grid = grid_for(agents) if grid is None else grid
     hours = 24 * days + 1
     u = latin_hypercube(runs, len(PARAMS), seed)
     cfgs = [config_for(d, agents, grid, hours, seed=seed * 1_000_003 + i, per_agents=per_agents)
@@ -175,6 +177,18 @@ def screened_sweep(net, candidates: int = 65_536, keep: int = 256, replicates: i
     screened_s = t_screen + t_abm_screened
     top = np.argsort(err_s)[:8]
     top_r = np.argsort(err_r)[:8]
+
+    def per_param(u: np.ndarray) -> dict:
+        """|recovered - hidden| per parameter, in units of its range."""
+        return {p.name: round(float(abs(u[k] - hidden[0, k])), 4) for k, p in enumerate(PARAMS)}
+
+    def fit_weighted(points: np.ndarray, errs: np.ndarray) -> np.ndarray:
+        """Mean of the best eight candidates weighted by 1 / curve error."""
+        w = 1.0 / np.maximum(errs, 1e-30)
+        return (points * w[:, None]).sum(axis=0) / w.sum()
+
+    est_s = fit_weighted(cand[rerun][top], err_s[top])
+    est_r = fit_weighted(cand[rand_idx][top_r], err_r[top_r])
     return {
         "candidates": candidates, "keep": n_kept, "replicates": replicates, "agents": agents, "grid": grid,
         "days": days, "target_abm_s": t_target, "screen_s": t_screen, "abm_screened_s": t_abm_screened,
@@ -192,7 +206,11 @@ def screened_sweep(net, candidates: int = 65_536, keep: int = 256, replicates: i
         "screened_top8_param_err_mean": float(unit_distance(cand[rerun][top], hidden).mean()),
         "screened_best_curve_mse": float(err_s[pick]),
         "screened_best_peak_rel_err_vs_target": float(relative_peak_error(mean_s[pick:pick + 1], target[None], days)[0]),
+        "screened_best_param_abs_err": per_param(cand[rerun][pick]),
+        "screened_top8_weighted_param_err": float(unit_distance(est_s, hidden)[0]),
+        "screened_top8_weighted_param_abs_err": per_param(est_s),
         "abm_only_best_param_err": float(unit_distance(cand[rand_idx][pick_r], hidden)[0]),
+        "abm_only_top8_weighted_param_err": float(unit_distance(est_r, hidden)[0]),
         "abm_only_top8_param_err_mean": float(unit_distance(cand[rand_idx][top_r], hidden).mean()),
         "abm_only_best_curve_mse": float(err_r[pick_r]),
         "abm_only_best_peak_rel_err_vs_target": float(relative_peak_error(mean_r[pick_r:pick_r + 1], target[None],
