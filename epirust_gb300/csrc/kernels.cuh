@@ -320,9 +320,18 @@ __device__ __forceinline__ void decide_body(const DevParams* __restrict__ Pall, 
     }
     bool ended = false;
     const uint32_t grp = kEnsembleChunkGroup;  // chunks per stride step
-    for (uint32_t c = blockIdx.x * grp, k = 0; c < n_chunks;
-         c = (++k < grp) ? c + 1u : c + (gridDim.x - 1u) * grp + 1u, k = (k < grp) ? k : 0u) {
-        const uint32_t r = chunk_rep[c];
+    // The replicate of the next chunk is read one chunk ahead, and a chunk's agent words are
+    // read before its replicate is known (every chunk of an ensemble is whole in the slot
+    // arrays), so neither waits on the other.
+    auto next_chunk = [&](uint32_t c, uint32_t k) { return k + 1u < grp ? c + 1u : c + (gridDim.x - 1u) * grp + 1u; };
+    uint32_t r_next = blockIdx.x * grp < n_chunks ? chunk_rep[blockIdx.x * grp] : 0u;
+    for (uint32_t c = blockIdx.x * grp, k = 0; c < n_chunks; c = next_chunk(c, k), k = (k + 1u < grp) ? k + 1u : 0u) {
+        const uint32_t r = r_next;
+        const uint32_t cn = next_chunk(c, k);
+        r_next = cn < n_chunks ? chunk_rep[cn] : 0u;
+        const uint32_t slot = c * kChunk + threadIdx.x;
+        const uint2 sv = st[slot];
+        const uint32_t pw = pos[slot], hw = home[slot], ww = work[slot];
         if (r != br.r) {
             switch_rep(br, r, Pall, sP, sh, row_ptr(ha, hr.row));
             hosp_known = false;
@@ -331,16 +340,9 @@ __device__ __forceinline__ void decide_body(const DevParams* __restrict__ Pall, 
         if (!P.active || ended) continue;
         const PlaneView pl{plane + P.plane_off, P.G, P.WP, err, danger ? danger + P.plane_off : nullptr};
         uint32_t* rclaim = claim + P.claim_off;
-        const uint32_t slot = c * kChunk + threadIdx.x;
         const uint32_t i = slot - P.agent_off;  // index within the replicate
         const bool valid = i < P.n;
-        uint32_t s = 0, at = 0, p = 0;
-        if (valid) {
-            const uint2 sv = st[slot];
-            s = sv.x;
-            at = sv.y;
-            p = pos[slot];
-        }
+        const uint32_t s = valid ? sv.x : 0u, at = valid ? sv.y : 0u, p = valid ? pw : 0u;
         if (HC == kHcStart) {
             const bool need = valid && wants_hospital(P, infected(s) ? with_day(s, st_day(s) + 1u) : s);
             if (__syncthreads_or(need) && !hosp_known) {
@@ -348,8 +350,8 @@ __device__ __forceinline__ void decide_body(const DevParams* __restrict__ Pall, 
                 hosp_known = true;
             }
         }
-        const uint32_t bin = valid ? decide_agent<HC>(P, pl, rclaim, wsa, st, tgt, lost, slot, i, s, at, p, home[slot],
-                                                      work[slot], hour, hod, hosp_first, err)
+        const uint32_t bin = valid ? decide_agent<HC>(P, pl, rclaim, wsa, st, tgt, lost, slot, i, s, at, p, hw, ww, hour,
+                                                      hod, hosp_first, err)
                                    : 0u;
         count_into(sh, valid, bin);
     }
