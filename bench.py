@@ -179,6 +179,17 @@ def cpu_baseline(cfg: dict, records, seconds: float = 12.0, max_hours: int = 240
             sim.run(1 + h, 2 + h, interventions=True, stop=False)
             h += 1
         variants[name] = {"value": n * h / (time.perf_counter() - t0), "hours": h}
+    # the reference's own default world (10,000 agents, 250 grid, small pox, 2,400 h) run in full
+    # by the same port on all cores, world from the oracle's build
+    with open(os.path.join(ROOT, "tests", "golden", "small_pox_10k_250.json")) as f:
+        c1 = json.load(f)
+    p1 = oracle.params_from_config(c1)
+    recs1 = oracle.O1(p1).export()
+    sim = oracle.O2(p1, recs1, threads=threads)
+    t0 = time.perf_counter()
+    rows = sim.run(1, int(c1["hours"]), interventions=True, stop=True)
+    variants["o2_config1_full_run"] = {"value": len(recs1) * len(rows) / (time.perf_counter() - t0),
+                                       "hours": len(rows), "agents": len(recs1), "threads": threads}
     out["variants"] = variants
     return out
 
