@@ -250,6 +250,44 @@ __device__ __forceinline__ Cell goto_area(const PlaneView& pl, uint32_t s, const
     return move_agent_from(pl, s, cur, cell, dr);
 }
 
+// One lane of an hour whose arms mix a jump and a walk, as one code path: jump lanes take
+// goto_area of a worker (Normal or Essential: a random point of the target area, kept when
+// vacant), walk lanes move_agent_from over the current area.  Both read the plane row through
+// their centre cell in the same pass (a jump tests its centre byte); walkers also read the
+// rows above and below.  Same words and outcomes as the two calls, without a warp running the
+// two arms' loads one after the other.  Used for hour 8 (workers to the office, the others a
+// walk): its k_decide went from 25.9 to 23.6 us at 1M agents.  In hours 7, 16 and 17 the two
+// plain calls were measured as fast.
+__device__ __forceinline__ Cell jump_or_walk(const PlaneView& pl, uint32_t s, bool jump, const Rect& cur,
+                                             const Rect& target, uint32_t home, uint32_t work, Cell cell, Draws& dr) {
+    bool act = can_move(s);
+    if (jump && !act) {  // goto_area's symptomatic override of a worker going home from the office
+        const uint32_t v = s & kStateMask;
+        act = rect_has(office_rect(work), cell.x, cell.y) && rect_eq(target, home_rect(home)) &&
+              (v == EPI_I_MILD || v == EPI_I_SEVERE);
+    }
+    if (!act) return cell;
+    Cell c = cell;
+    if (jump || !rect_has(cur, cell.x, cell.y)) c = random_point(jump ? target : cur, dr.m(0), dr.m(1));
+    if (!pl.inside(c.x, c.y)) {  // reads as occupied (and is reported), as rows_around and vacant do
+        atomicOr(pl.err, 1);
+        return cell;
+    }
+    const uint32_t r1 = pl.row3(c.x, c.y);
+    uint32_t r0 = 0u, r2 = 0u;
+    if (!jump) {
+        r0 = pl.row3(c.x, c.y - 1);
+        r2 = pl.row3(c.x, c.y + 1);
+    }
+    if (jump) return ((r1 >> 8) & 0xFFu) == 0u ? c : cell;
+    const uint32_t u = dr.m(2);
+    const uint32_t cand = valid_neighbours(cur, pl.G, c.x, c.y) & ~occupied_mask(Rows3{r0, r1, r2});
+    if (!cand) return cell;
+    const uint32_t j = uniform_index(u, (uint32_t)__popc(cand));
+    const uint32_t e = __ldg(&kStepTable.v[cand][j]);
+    return Cell{c.x + (int32_t)(e & 3u) - 1, c.y + (int32_t)(e >> 2) - 1};
+}
+
 // DiseaseStateMachine::next with the default DiseaseHandler (ddh:41-86) for the hour's
 // proposed cell; at is the Exposed/Pre at_hour word.
 // (The agent's current area, needed only when an infectious neighbour exists, is decoded from
@@ -367,33 +405,36 @@ __device__ __forceinline__ Cell perform_movements(const DevParams& P, const Plan
     } else {
         const Rect cur = area_rect(P, st_area(s), home, work);
         const bool worker = ws != EPI_WS_NA;  // Normal or Essential here
-        if (HC != kHcMove)  // the arm below that goes to an area draws a random point, the other walks
-            dr.prime(HC == kHcTransport ? worker && (s & kPt) : HC == kHcWork ? true : HC == kHcNoon ? !worker : worker);
+        // The arms of each class, as goto_area / move_agent_from calls of the reference.  A
+        // non-worker's goto_area is move_agent_from over its current area (work status NA), so
+        // a class's arms are a jump of some workers and a walk of everyone else (at noon, a
+        // walk of everyone: one call).  Where lanes differ, each computes its one Philox block
+        // before the branch, the point block for a jump and the choice block for a walk, so a
+        // warp runs the rounds once.
         if (HC == kHcMove) {
             nc = move_agent_from(pl, s, cur, cell, dr);
         } else if (HC == kHcTransport) {
-            if (worker && (s & kPt)) {
+            // worker with public transport: goto_area(transport); others: move_agent_from
+            const bool jump = worker && (s & kPt);
+            dr.prime(jump);
+            if (jump) {
                 nc = goto_area(pl, s, cur, P.area[kTransport], home, work, cell, dr);
                 s = with_area(s, kTransport);
             } else {
                 nc = move_agent_from(pl, s, cur, cell, dr);
             }
         } else if (HC == kHcWork) {
-            if (worker) {
-                nc = goto_area(pl, s, cur, office_rect(work), home, work, cell, dr);
-                s = with_area(s, kWork);
-            } else {
-                nc = goto_area(pl, s, cur, P.area[kHousing], home, work, cell, dr);
-                s = with_area(s, kHousing);
-            }
+            // worker: goto_area(office); non-worker: goto_area(housing), a walk
+            dr.prime(worker);
+            nc = jump_or_walk(pl, s, worker, cur, office_rect(work), home, work, cell, dr);
+            s = with_area(s, worker ? kWork : kHousing);
         } else if (HC == kHcNoon) {
-            if (worker) {
-                nc = move_agent_from(pl, s, cur, cell, dr);
-            } else {
-                nc = goto_area(pl, s, cur, home_rect(home), home, work, cell, dr);
-                s = with_area(s, kHome);
-            }
+            // worker: move_agent_from; non-worker: goto_area(home), a walk
+            nc = move_agent_from(pl, s, cur, cell, dr);
+            if (!worker) s = with_area(s, kHome);
         } else {  // kHcHome
+            // worker: goto_area(home); non-worker: move_agent_from
+            dr.prime(worker);
             if (worker) {
                 nc = goto_area(pl, s, cur, home_rect(home), home, work, cell, dr);
                 s = with_area(s, kHome);
