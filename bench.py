@@ -517,7 +517,7 @@ def run_gpu(args, cfg):
                                           "3 B (hours 1-6), 12 B (hour 23), reference-layout accounting"},
                          "kernels": {k: {"launches": v[0], "ms": v[1]} for k, v in stats.items() if v[0]}},
             "cpu_baseline": cpu,
-            "e2e": {"value": e2e_value, "unit": METRIC, "h2d_bytes_per_step": int(n * 24),
+            "e2e": {"value": e2e_value, "unit": METRIC, "h2d_bytes_per_step": int(host_records.nbytes),
                     "d2h_bytes_per_step": int(hours_per_step * 32), "steps": e2e_steps},
             "gpu_launches": int(launches),
             "clocks": clocks,

@@ -201,17 +201,6 @@ static DevParams make_dev_params(const epi_params& p, const epi_geography& geo0,
     return d;
 }
 
-static uint32_t area_code_of(const DevParams& hp, const epi_agent_record& r, bool* ok) {
-    Rect a{r.area_x0, r.area_y0, r.area_x1, r.area_y1};
-    *ok = true;
-    if (rect_eq(a, Rect{r.home_x, r.home_y, r.home_x + 1, r.home_y + 1})) return kHome;
-    if (r.work_status != EPI_WS_NA && rect_eq(a, Rect{r.work_x, r.work_y, r.work_x + 9, r.work_y + 9})) return kWork;
-    for (uint32_t c = kTransport; c < kNumAreas; ++c)
-        if (rect_eq(a, hp.area[c])) return c;
-    *ok = false;
-    return kHome;
-}
-
 // ------------------------------------------------------------------ launch bookkeeping
 // Eagerly launched kernels take their event pair from the pool and return it once read;
 // kernels captured into a profiling graph get a pair of their own, recorded as external
@@ -842,53 +831,6 @@ static void free_device(epi_engine* h) {
 
 static size_t align_up(size_t v, size_t a) { return (v + a - 1) / a * a; }
 
-// Pack one replicate's records into the host mirrors of the SoA arrays.
-// Records i0 .. i1 - 1 of replicate r.
-static int pack_replica(const epi_engine* h, uint32_t r, const epi_agent_record* recs, uint32_t* pos, uint2* st,
-                        uint32_t* home, uint32_t* work, uint32_t* wsa, std::string& err, uint32_t i0 = 0,
-                        uint32_t i1 = 0xFFFFFFFFu) {
-    const Replica& rep = h->reps[r];
-    const int32_t G = (int32_t)rep.p.grid_size;
-    auto inside = [G](int32_t x0, int32_t y0, int32_t x1, int32_t y1) {
-        return x0 >= 0 && y0 >= 0 && x1 <= G && y1 <= G && x0 <= x1 && y0 <= y1;
-    };
-    for (uint32_t i = i0; i < std::min(i1, rep.n); ++i) {
-        const epi_agent_record& a = recs[i];
-        if (a.x < 0 || a.y < 0 || a.x > G || a.y > G || a.state > EPI_D || a.work_status > EPI_WS_NA ||
-            a.immunity < -2 || a.immunity > 2 || a.infection_day > 0xFFFFu ||
-            !inside(a.home_x, a.home_y, a.home_x + 1, a.home_y + 1) ||
-            (a.work_status != EPI_WS_NA && !inside(a.work_x, a.work_y, a.work_x + 9, a.work_y + 9)) ||
-            !inside(a.area_x0, a.area_y0, a.area_x1, a.area_y1)) {
-            err = "replicate " + std::to_string(r) + ": agent record " + std::to_string(i) + " out of range";
-            return EPI_ERR_ARG;
-        }
-        bool ok = true;
-        const uint32_t code = area_code_of(rep.hp, a, &ok);
-        if (!ok) {
-            err = "replicate " + std::to_string(r) + ": agent record " + std::to_string(i) +
-                  ": current area is not one of its areas";
-            return EPI_ERR_ARG;
-        }
-        uint32_t s = (uint32_t)a.state;
-        if (a.flags & EPI_F_HOSPITALIZED) s |= kHosp;
-        if (a.flags & EPI_F_ISOLATED) s |= kIso;
-        if (a.flags & EPI_F_VACCINATED) s |= kVacc;
-        if (a.flags & EPI_F_WORK_QUARANTINED) s |= kWq;
-        if (a.flags & EPI_F_PUBLIC_TRANSPORT) s |= kPt;
-        s |= code << kAreaShift;
-        s |= (uint32_t)a.work_status << kWsShift;
-        s |= (uint32_t)(a.immunity + 2) << kImmShift;
-        s |= a.infection_day << kDayShift;
-        const size_t slot = rep.hp.agent_off + i;
-        st[slot] = make_uint2(s, a.at_hour);
-        pos[slot] = pack_xy(a.x, a.y);
-        home[slot] = pack_xy(a.home_x, a.home_y);
-        work[slot] = pack_xy(a.work_x, a.work_y);
-        wsa[slot] = a.work_start_at;
-    }
-    return EPI_OK;
-}
-
 static int finish_upload(epi_engine* h);
 
 // World build on the device (world.cuh) for every replicate, from the host plan.
@@ -1052,35 +994,35 @@ static int engine_init(epi_engine* h, const epi_params* params, const epi_agent_
         if (rc) return rc;
         return finish_upload(h);
     }
-    // host mirrors, filled in parallel: pieces of at most 64K records of any replicate
-    std::vector<uint32_t> pos(slots, 0), home(slots, 0), work(slots, 0), wsa(slots, 0);
-    std::vector<uint2> st(slots, make_uint2(0, 0));
-    constexpr uint32_t kPackPiece = 1u << 16;
-    std::vector<std::pair<uint32_t, uint32_t>> pieces;  // (replicate, first record)
+    // The records go to the device as they are (replicate r's at slot agent_off(r)) and
+    // k_pack_records checks and packs them there; the first bad one is reported.
+    rc = push_params(h);
+    if (rc) return rc;
+    struct DeviceBuffer {
+        void* p = nullptr;
+        ~DeviceBuffer() { if (p) cudaFree(p); }
+    } stage;
+    CK(cudaMalloc(&stage.p, slots * sizeof(epi_agent_record)));
+    epi_agent_record* d_recs = static_cast<epi_agent_record*>(stage.p);
     for (uint32_t r = 0; r < R; ++r)
-        for (uint32_t i = 0; i < h->reps[r].n; i += kPackPiece) pieces.emplace_back(r, i);
-    std::vector<int> status(pieces.size(), EPI_OK);
-    std::vector<std::string> errs(pieces.size());
-    const unsigned workers =
-        std::max(1u, std::min<unsigned>((unsigned)pieces.size(), std::thread::hardware_concurrency()));
-    std::vector<std::thread> pool;
-    for (unsigned w = 0; w < workers; ++w)
-        pool.emplace_back([&, w] {
-            for (size_t k = w; k < pieces.size(); k += workers) {
-                const uint32_t r = pieces[k].first, i0 = pieces[k].second;
-                status[k] = pack_replica(h, r, recs[r], pos.data(), st.data(), home.data(), work.data(), wsa.data(),
-                                         errs[k], i0, i0 + kPackPiece);
-            }
-        });
-    for (auto& t : pool) t.join();
-    for (size_t k = 0; k < pieces.size(); ++k)  // the first bad record in (replicate, index) order
-        if (status[k]) { h->err = errs[k]; return status[k]; }
-    CK(cudaMemcpyAsync(h->d_pos, pos.data(), slots * sizeof(uint32_t), cudaMemcpyHostToDevice, h->stream));
-    CK(cudaMemcpyAsync(h->d_home, home.data(), slots * sizeof(uint32_t), cudaMemcpyHostToDevice, h->stream));
-    CK(cudaMemcpyAsync(h->d_work, work.data(), slots * sizeof(uint32_t), cudaMemcpyHostToDevice, h->stream));
-    CK(cudaMemcpyAsync(h->d_wsa, wsa.data(), slots * sizeof(uint32_t), cudaMemcpyHostToDevice, h->stream));
-    CK(cudaMemcpyAsync(h->d_st, st.data(), slots * sizeof(uint2), cudaMemcpyHostToDevice, h->stream));
-    CK(cudaStreamSynchronize(h->stream));  // the host mirrors go out of scope
+        CK(cudaMemcpyAsync(d_recs + h->reps[r].hp.agent_off, recs[r], (size_t)h->reps[r].n * sizeof(epi_agent_record),
+                           cudaMemcpyHostToDevice, h->stream));
+    CK(cudaMemsetAsync(h->d_scratch, 0xFF, sizeof(unsigned long long), h->stream));
+    k_pack_records<<<blocks_for(h->slots), kThreads, 0, h->stream>>>(h->d_params, h->d_chunk_rep, h->slots, d_recs,
+                                                                     h->d_pos, h->d_st, h->d_home, h->d_work, h->d_wsa,
+                                                                     h->d_scratch);
+    CK(cudaGetLastError());
+    unsigned long long bad = ~0ull;
+    CK(cudaMemcpyAsync(&bad, h->d_scratch, sizeof bad, cudaMemcpyDeviceToHost, h->stream));
+    CK(cudaStreamSynchronize(h->stream));
+    if (bad != ~0ull) {  // the replicate holding the slot, and the record's index within it
+        const uint64_t slot = bad >> 1;
+        uint32_t r = 0;
+        while (r + 1 < R && h->reps[r + 1].hp.agent_off <= slot) ++r;
+        h->err = "replicate " + std::to_string(r) + ": agent record " + std::to_string(slot - h->reps[r].hp.agent_off) +
+                 ((bad & 1u) ? ": current area is not one of its areas" : " out of range");
+        return EPI_ERR_ARG;
+    }
     return finish_upload(h);
 }
 

@@ -110,6 +110,56 @@ struct DevParams {
 
 constexpr uint32_t kGuardLock = 1u, kGuardSpread = 2u, kGuardOccupancy = 4u;
 
+// Code of an agent record's current_area: its house, its office (workers), or the global area
+// with the same rectangle; ok = false when it is none of them.
+EPI_HD uint32_t area_code_of(const DevParams& hp, const epi_agent_record& r, bool* ok) {
+    const Rect a{r.area_x0, r.area_y0, r.area_x1, r.area_y1};
+    *ok = true;
+    if (rect_eq(a, Rect{r.home_x, r.home_y, r.home_x + 1, r.home_y + 1})) return kHome;
+    if (r.work_status != EPI_WS_NA && rect_eq(a, Rect{r.work_x, r.work_y, r.work_x + 9, r.work_y + 9})) return kWork;
+    for (uint32_t c = kTransport; c < kNumAreas; ++c)
+        if (rect_eq(a, hp.area[c])) return c;
+    *ok = false;
+    return kHome;
+}
+
+// The SoA words of one agent record (the host layout), with the checks that
+// epi_engine_create_from_records documents.  Returns 0 when packed, 1 when a field is out of
+// range (a cell outside [0, G], a house, office or current area reaching outside the plane, a
+// state, work status, immunity or infection day beyond its field), 2 when the current area is
+// none of the agent's areas.
+struct AgentWords {
+    uint32_t pos, s, at, home, work, wsa;
+};
+EPI_HD bool rect_in_plane(int32_t G, int32_t x0, int32_t y0, int32_t x1, int32_t y1) {
+    return x0 >= 0 && y0 >= 0 && x1 <= G && y1 <= G && x0 <= x1 && y0 <= y1;
+}
+EPI_HD int record_words(const DevParams& hp, const epi_agent_record& a, AgentWords& w) {
+    const int32_t G = hp.G;
+    if (a.x < 0 || a.y < 0 || a.x > G || a.y > G || a.state > EPI_D || a.work_status > EPI_WS_NA ||
+        a.immunity < -2 || a.immunity > 2 || a.infection_day > 0xFFFFu ||
+        !rect_in_plane(G, a.home_x, a.home_y, a.home_x + 1, a.home_y + 1) ||
+        (a.work_status != EPI_WS_NA && !rect_in_plane(G, a.work_x, a.work_y, a.work_x + 9, a.work_y + 9)) ||
+        !rect_in_plane(G, a.area_x0, a.area_y0, a.area_x1, a.area_y1))
+        return 1;
+    bool ok = true;
+    const uint32_t code = area_code_of(hp, a, &ok);
+    if (!ok) return 2;
+    uint32_t s = (uint32_t)a.state;
+    if (a.flags & EPI_F_HOSPITALIZED) s |= kHosp;
+    if (a.flags & EPI_F_ISOLATED) s |= kIso;
+    if (a.flags & EPI_F_VACCINATED) s |= kVacc;
+    if (a.flags & EPI_F_WORK_QUARANTINED) s |= kWq;
+    if (a.flags & EPI_F_PUBLIC_TRANSPORT) s |= kPt;
+    s |= code << kAreaShift;
+    s |= (uint32_t)a.work_status << kWsShift;
+    s |= (uint32_t)(a.immunity + 2) << kImmShift;
+    s |= a.infection_day << kDayShift;
+    w = AgentWords{pack_xy(a.x, a.y), s, a.at_hour, pack_xy(a.home_x, a.home_y), pack_xy(a.work_x, a.work_y),
+                   a.work_start_at};
+    return 0;
+}
+
 constexpr uint32_t kChunk = 256;  // agent slots per chunk; replicates start on chunk boundaries
 
 // Bernoulli(p) as a threshold on a uniform 32-bit word: gen_bool(p) <=> u < thr.

@@ -155,5 +155,34 @@ __global__ void k_world_infect(const uint4* __restrict__ list, uint32_t count, u
     }
 }
 
+// Caller-supplied agent records (the host layout, copied to the device as they are, record i
+// of replicate r at slot agent_off(r) + i) into the SoA words, one slot per thread; slots past
+// a replicate's agents are zeroed.  A record that fails record_words leaves slot << 1 |
+// (kind - 1) in *bad by atomicMin, so *bad names the first bad record in (replicate, index)
+// order.
+__global__ void __launch_bounds__(kThreads) k_pack_records(const DevParams* __restrict__ Pall,
+                                                           const uint32_t* __restrict__ chunk_rep, uint32_t n_slots,
+                                                           const epi_agent_record* __restrict__ recs,
+                                                           uint32_t* __restrict__ pos, uint2* __restrict__ st,
+                                                           uint32_t* __restrict__ home, uint32_t* __restrict__ work,
+                                                           uint32_t* __restrict__ wsa, unsigned long long* __restrict__ bad) {
+    for (uint32_t slot = blockIdx.x * blockDim.x + threadIdx.x; slot < n_slots; slot += gridDim.x * blockDim.x) {
+        const DevParams& P = Pall[chunk_rep ? chunk_rep[slot / kChunk] : 0u];
+        AgentWords w{0u, 0u, 0u, 0u, 0u, 0u};
+        if (slot - P.agent_off < P.n) {
+            const int kind = record_words(P, recs[slot], w);
+            if (kind) {
+                atomicMin(bad, ((unsigned long long)slot << 1) | (unsigned long long)(kind - 1));
+                w = AgentWords{0u, 0u, 0u, 0u, 0u, 0u};
+            }
+        }
+        pos[slot] = w.pos;
+        st[slot] = make_uint2(w.s, w.at);
+        home[slot] = w.home;
+        work[slot] = w.work;
+        wsa[slot] = w.wsa;
+    }
+}
+
 }  // namespace kern
 }  // namespace epi

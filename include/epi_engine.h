@@ -221,7 +221,12 @@ int epi_engine_create(const epi_params* params, epi_engine** out);
 /* Same, from the JSON config text; seed overrides the config's optional "seed" key. */
 int epi_engine_create_json(const char* config_json, uint64_t seed, epi_engine** out);
 
-/* Same, from host-side records (a world built elsewhere or a checkpoint). */
+/* Same, from host-side records (a world built elsewhere or a checkpoint).  The records are
+ * copied to the device as they are (pinned host memory makes that one DMA) and checked and
+ * packed there: a cell, house, office or current area outside [0, grid_size], a state, work
+ * status, immunity or infection day beyond its field, or a current area that is none of the
+ * agent's areas returns EPI_ERR_ARG, and epi_engine_last_error(NULL) names the first such
+ * record. */
 int epi_engine_create_from_records(const epi_params* params, const epi_agent_record* recs,
                                    size_t n, epi_engine** out);
 

@@ -221,6 +221,57 @@ def test_records_roundtrip(gpu, oracle_mod):
     _assert_same_agents(eng, sim2, "continued")
 
 
+def test_bad_records_are_refused(gpu, oracle_mod):
+    """Records are checked where they are packed, on the device: a field out of range or a
+    current area that is none of the agent's areas refuses the engine with EPI_ERR_ARG, and
+    the message names the first bad record in index order.  Good records still load."""
+    from epirust_gb300 import _lib
+
+    cfg = make_config(n=3000, grid=120, seed=12, disease=COVID_FAST, starting=(10, 10, 10, 30))
+    good = _oracle(oracle_mod, cfg).export()
+    G = cfg["geography_parameters"]["grid_size"]
+    worker = int(np.flatnonzero(good["work_status"] != 3)[0])
+
+    def refused(edit):
+        recs = good.copy()
+        edit(recs)
+        with pytest.raises(_lib.EpiError) as e:
+            _engine(cfg, records=recs)
+        assert e.value.code == 6
+        return str(e.value)
+
+    def set_(field, k, v):
+        return lambda r: r[field].__setitem__(k, v)
+
+    assert "agent record 17 out of range" in refused(set_("x", 17, G + 1))
+    assert "agent record 3 out of range" in refused(set_("immunity", 3, 3))
+    assert "agent record 40 out of range" in refused(set_("state", 40, 8))
+    assert "agent record 2999 out of range" in refused(set_("home_y", 2999, G))
+    assert f"agent record {worker} out of range" in refused(set_("work_x", worker, G - 5))
+
+    def shift_area(k):
+        def edit(r):
+            r["area_x0"][k] += 1
+            r["area_x1"][k] += 1
+        return edit
+
+    msg = refused(shift_area(5))
+    assert "replicate 0: agent record 5: current area is not one of its areas" in msg
+
+    def two(r):  # the lower index is reported, whatever its kind
+        shift_area(9)(r)
+        r["y"][30] = -1
+    assert "agent record 9: current area" in refused(two)
+
+    def two_b(r):
+        shift_area(31)(r)
+        r["y"][30] = -1
+    assert "agent record 30 out of range" in refused(two_b)
+
+    eng = _engine(cfg, records=good)
+    _assert_same_agents(eng, _oracle(oracle_mod, cfg), "loaded")
+
+
 def test_full_size_world_first_day_parity(gpu, oracle_mod):
     """The 1M-agent / 2,500-grid world: the first 30 hours equal the oracle."""
     cfg = golden("small_pox_1m_2500.json")
