@@ -386,15 +386,17 @@ int ensure_predict(epi_mlp* h, uint32_t n_pad) {
 }
 
 // Forward pass of n host samples through every member; outputs stay in d_py (and scores in
-// d_pscore when target).
+// d_pscore when target).  The buffers hold p_cap rows per member (the largest call so far):
+// member m's rows start at m * p_cap in every buffer and tensor map, whatever n is.
 int forward_n(epi_mlp* h, const float* x, uint32_t n, const float* target) {
     const uint32_t n_pad = std::max<uint32_t>(round_up(n, kBM), kBM);
     MRC(ensure_predict(h, n_pad));
+    const uint64_t cap = h->p_cap;
     std::vector<__nv_bfloat16> xs = pad_inputs(x, n, n_pad, h->cfg.in_dim);
     MCK(cudaMemcpyAsync(h->layers[0].ph, xs.data(), xs.size() * sizeof(__nv_bfloat16), cudaMemcpyHostToDevice, h->stream));
     if (target) {
         MCK(cudaMemcpyAsync(h->d_ptarget, target, h->cfg.out_dim * sizeof(float), cudaMemcpyHostToDevice, h->stream));
-        MCK(cudaMemsetAsync(h->d_pscore, 0, (size_t)h->E * n_pad * sizeof(float), h->stream));
+        MCK(cudaMemsetAsync(h->d_pscore, 0, (size_t)h->E * cap * sizeof(float), h->stream));
     }
     for (uint32_t l = 0; l < h->L; ++l) {
         MlpLayer& ly = h->layers[l];
@@ -404,7 +406,7 @@ int forward_n(epi_mlp* h, const float* x, uint32_t n, const float* target) {
         const uint32_t za = l == 0 ? 0u : 1u;  // the input rows are shared
         if (l + 1 < h->L) {
             a.out = h->layers[l + 1].ph;
-            a.ms_out = (uint64_t)n_pad * ly.N;
+            a.ms_out = cap * ly.N;
             MRC((gemm<128, kEpHidden>(h, ly.t_ph, ly.t_w, n_pad, ly.N, ly.K, a, za)));
         } else {
             a.outf = target ? nullptr : h->d_py;
@@ -412,8 +414,8 @@ int forward_n(epi_mlp* h, const float* x, uint32_t n, const float* target) {
             a.score = target ? h->d_pscore : nullptr;
             a.n_valid = h->cfg.out_dim;
             a.m_valid = n;
-            a.ms_outf = (uint64_t)n_pad * ly.N;
-            a.ms_score = n_pad;
+            a.ms_outf = cap * ly.N;
+            a.ms_score = cap;
             MRC((gemm<128, kEpOut>(h, ly.t_ph, ly.t_w, n_pad, ly.N, ly.K, a, za)));
         }
     }

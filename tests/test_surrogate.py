@@ -132,6 +132,29 @@ def test_forward_matches_oracle(gpu, n):
 
 
 @pytest.mark.gpu
+def test_smaller_calls_after_larger_ones(gpu):
+    """A handle's prediction buffers keep the rows of its largest call so far.  Predictions of a
+    later, smaller call equal, member for member and bit for bit, those of a fresh handle and
+    the same rows of the larger call (every member's rows start at the same place in every
+    buffer, whatever the call's size); so do scores, up to the order in which the output tiles'
+    partial sums are added (relative 1e-5)."""
+    rng = np.random.default_rng(5)
+    x = rng.random((1000, 8))
+    target = rng.random(600)
+    a, b = _net(gpu, seed=2, members=3), _net(gpu, seed=2, members=3)
+    big = a.predict_members(x)
+    big_score = a.score_members(x, target)
+    for n in (100, 300, 129):
+        small = a.predict_members(x[:n])
+        assert np.array_equal(small, big[:, :n]), n
+        assert np.allclose(a.score_members(x[:n], target), big_score[:, :n], rtol=1e-5, atol=0), n
+    assert np.array_equal(b.predict_members(x[:300]), big[:, :300])
+    assert np.allclose(b.score_members(x[:129], target), big_score[:, :129], rtol=1e-5, atol=0)
+    a.close()
+    b.close()
+
+
+@pytest.mark.gpu
 def test_gradients_match_oracle(gpu):
     """Loss and every layer's weight and bias gradients of one 256-sample minibatch.
     Tolerance: loss 1e-3 relative; gradients 2e-2 relative Frobenius per tensor (BF16 dZ
@@ -270,3 +293,40 @@ def test_members_equal_lone_networks(gpu):
     ens.set_params(pe[::-1].copy())
     assert np.array_equal(ens.get_params(), pe[::-1])
     ens.close()
+
+
+@pytest.mark.gpu
+def test_transfer_tune_fits_larger_worlds(gpu):
+    """transfer_tune: a copy of the ensemble (weights and output scaling bit for bit before any
+    step) fine-tuned on ABM runs of a ten times larger world predicts held-out curves of that
+    world better than the network trained on the small worlds alone."""
+    from epirust_gb300.surrogate import (Surrogate, compartment_scaling, config_for, denormalise, latin_hypercube,
+                                         simulate_curves, uniform_candidates)
+    from epirust_gb300.sweep import grid_for, transfer_tune
+
+    days, small, big = 20, 2000, 20000
+    hours = 24 * days + 1
+    u = latin_hypercube(640, 8, seed=11)
+    y = simulate_curves([config_for(d, small, grid_for(small), hours, seed=5000 + i, per_agents=small)
+                         for i, d in enumerate(denormalise(u))], days)
+    net = Surrogate(in_dim=8, out_dim=6 * days, hidden=256, hidden_layers=2, batch=128, seed=3, members=2)
+    net.set_output_scaling(*compartment_scaling(y, days))
+    net.set_dataset(u, y)
+    net.train(1000, seed=1)
+
+    ue = uniform_candidates(64, 8, seed=21)
+    copy, info0 = transfer_tune(net, agents=big, points=4, steps=0, days=days, seed=13, per_agents=small)
+    assert np.array_equal(copy.predict_members(ue), net.predict_members(ue))
+    assert np.array_equal(copy.get_params(), net.get_params())
+    copy.close()
+
+    tuned, info = transfer_tune(net, agents=big, points=256, steps=400, lr=2e-4, days=days, seed=13,
+                                per_agents=small, abm_batch=256)
+    assert info["points"] == 256 and info["agents"] == big and info["grid"] == grid_for(big) and info["abm_s"] > 0
+    yb = simulate_curves([config_for(d, big, grid_for(big), hours, seed=9000 + i, per_agents=small)
+                          for i, d in enumerate(denormalise(ue))], days)
+    mse_tuned = np.mean((tuned.predict(ue) - yb) ** 2)
+    mse_small = np.mean((net.predict(ue) - yb) ** 2)
+    assert mse_tuned < mse_small, (mse_tuned, mse_small)
+    tuned.close()
+    net.close()
