@@ -348,17 +348,20 @@ def run_batched(args, stream, flush) -> dict:
 def run_surrogate(args) -> dict:
     """Surrogate training on GPU-ABM ensembles (4,096 Latin-hypercube runs of 100,000 agents,
     100 days, 5 MLP members 8 -> 512 x 3 -> 600 trained with Adam in BF16 on the tensor cores)
-    and the screened sweep (65,536 candidates, the best `sweep_keep` and the fallback
-    candidates where the members disagree re-run at 1,000,000 agents with 8 replicates each;
-    an ABM-only sweep measured on the same budget of unscreened candidates)."""
+    and the screened sweep (the members fine-tuned on `sweep_transfer` runs of 1,000,000
+    agents; 65,536 candidates, the best `sweep_keep` and the fallback candidates where the
+    members disagree re-run at 1,000,000 agents with 8 replicates each; an ABM-only sweep
+    measured on the same budget of unscreened candidates)."""
     from epirust_gb300.sweep import screened_sweep, train_on_abm
 
     net, train = train_on_abm(runs=args.train_runs, held_out=args.train_runs // 8, steps=args.train_steps)
     train.pop("curves")
-    sweep = screened_sweep(net, keep=args.sweep_keep, replicates=args.sweep_replicates)
+    sweep = screened_sweep(net, keep=args.sweep_keep, replicates=args.sweep_replicates,
+                           transfer_points=args.sweep_transfer)
     net.close()
     sweep["note"] = ("abm_only_sweep_s_extrapolated = every candidate x replicates through the ABM at the rate "
-                     "measured on its sample (abm_only_sample_runs unscreened runs, the screened sweep's budget)")
+                     "measured on its sample (abm_only_sample_runs unscreened runs, the screened sweep's budget: "
+                     "re-runs and fine-tuning runs); screened_sweep_s counts the fine-tuning runs")
     return {"metric": "surrogate sweep speedup @<=5% peak err", "training": train, "sweep": sweep}
 
 
@@ -549,6 +552,8 @@ def main():
     ap.add_argument("--train-runs", type=int, default=4096)
     ap.add_argument("--train-steps", type=int, default=3000)
     ap.add_argument("--sweep-keep", type=int, default=256)
+    ap.add_argument("--sweep-transfer", type=int, default=512,
+                    help="1M-agent ABM runs the surrogate is fine-tuned on before the screen (0: none)")
     ap.add_argument("--sweep-replicates", type=int, default=8)
     args = ap.parse_args()
     with open(args.config) as f:
