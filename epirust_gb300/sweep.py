@@ -126,9 +126,10 @@ def transfer_tune(net, agents: int = 1_000_000, points: int = 512, steps: int = 
     `agents`-agent worlds: `points` Latin-hypercube parameter points run once each by the
     batched ABM at that size, then `steps` Adam steps at learning rate `lr` from net's weights
     (same output scaling, fresh moments).  Per-capita curves of a ten times larger world on a
-    grid of the same density are not those of the training worlds (at 1M agents the 100k-agent
-    network's peak height was off by 78 % median over uniform points, and by 3.3 % after 512
-    runs and 600 steps, against 3.0 % for a single 1M-agent run).  Returns (tuned, info)."""
+    grid of the same density are close to, but not the same as, those of the training worlds:
+    against 8-replicate ABM means at 1M agents the 100k-agent network's peak height was off by
+    4.2 % (median, uniformly drawn points) and 6.0 % (the candidates a sweep keeps), and by
+    3.2 % and 3.7 % after 512 runs and 600 steps.  Returns (tuned, info)."""
     grid = grid_for(agents)
     hours = 24 * days + 1
     u = latin_hypercube(points, len(PARAMS), seed)
