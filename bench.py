@@ -188,7 +188,7 @@ def cpu_baseline(cfg: dict, records, seconds: float = 12.0, max_hours: int = 240
     sim = oracle.O2(p1, recs1, threads=threads)
     t0 = time.perf_counter()
     rows = sim.run(1, int(c1["hours"]), interventions=True, stop=True)
-    variants["o2_config1_full_run"] = {"value": len(recs1) * len(rows) / (time.perf_counter() - t0),
+    variants["o2_default_world_full_run"] = {"value": len(recs1) * len(rows) / (time.perf_counter() - t0),
                                        "hours": len(rows), "agents": len(recs1), "threads": threads}
     out["variants"] = variants
     return out

@@ -1,4 +1,4 @@
-"""Generate the reference-order-semantics sample for the distributional test of config 1.
+"""Generate the reference-order-semantics sample for the distributional test of the default world.
 
 TEST INFRASTRUCTURE ONLY: runs O2 (oracle/o2.c: FNV hash map keyed by cell, map phase over
 the map, serial first-come resolve in hash order, swap -- the data flow of

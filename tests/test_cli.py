@@ -58,7 +58,7 @@ def _outputs(out_dir):
 
 @pytest.mark.gpu
 def test_default_world_run_equals_oracle(gpu, engine_built, oracle_mod, tmp_path):
-    """Config 1 (the reference's default world: 10,000 agents, 250 grid, small pox,
+    """The reference's default world (10,000 agents, 250 grid, small pox,
     2,400 hours) through the binary: every CSV row equals the oracle's."""
     cfg = golden("small_pox_10k_250.json")
     path = tmp_path / "config.json"

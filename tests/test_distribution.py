@@ -8,8 +8,8 @@ of the engine semantics (lowest index wins; O1 on the CPU, the CUDA engine on th
 match O2's: peak height, peak day and final attack rate agree within a 4-sigma band of the
 difference of means, and a two-sample Kolmogorov-Smirnov test does not reject (p > 1e-3).
 
-Two workloads: config 1 of the benchmarks (small_pox_10k_250.json: 10,000 agents on a 250
-grid, small pox, 5 exposed, 2,400 hours), against 200 O2 runs that
+Two workloads: the reference's default world (small_pox_10k_250.json: 10,000 agents on a
+250 grid, small pox, 5 exposed, 2,400 hours), against 200 O2 runs that
 tests/golden/make_distribution_goldens.py committed; and a faster, denser disease on a 2,000
 agent world with a lockdown, whose 200 O2 runs are made live.
 """
@@ -120,7 +120,7 @@ def _golden_module():
     return mod
 
 
-def test_config1_o2_sample_is_complete():
+def test_default_world_o2_sample_is_complete():
     with open(os.path.join(GOLDEN, "o2_small_pox_10k_250_200.json")) as f:
         g = json.load(f)
     runs = np.array(g["runs"], dtype=np.float64)
@@ -129,8 +129,8 @@ def test_config1_o2_sample_is_complete():
 
 
 @pytest.mark.gpu
-def test_engine_matches_reference_order_semantics_config1(gpu):
-    """Config 1 (small pox, 10,000 agents, 250 grid, 2,400 h): the GPU engine over 200 seeds
+def test_engine_matches_reference_order_semantics_default_world(gpu):
+    """The default world (small pox, 10,000 agents, 250 grid, 2,400 h): the GPU engine over 200 seeds
     (1000..1199, one 200-replicate ensemble; each replicate equals a lone engine bit for bit)
     against the committed O2 sample (seeds 5000..5199): peak of active cases, its day and the
     final attack rate."""

@@ -60,7 +60,7 @@ def test_ensemble_rerun_from_saved_state_repeats(gpu):
         assert (a == b).all()
 
 
-def test_config3_shapes_small(gpu):
+def test_replicate_generator_shapes_small(gpu):
     """The 256-replicate generator (log-uniform populations, sqrt grids) at 16 small replicates."""
     from epirust_gb300 import Ensemble, Epidemiology
     from epirust_gb300.workloads import ensemble_params
