@@ -71,7 +71,12 @@ struct epi_engine {
     uint32_t *d_pos = nullptr, *d_home = nullptr, *d_work = nullptr, *d_wsa = nullptr, *d_tgt = nullptr;
     uint32_t* d_lost = nullptr;  // per slot: the hour in which the agent's claim was beaten
     uint2* d_st = nullptr;
+    // Byte planes of all replicates (plane_bytes).  A lone world keeps two (two_planes): the
+    // hours of day 7..22 rebuild the plane in the other one, and plane_par names the one
+    // holding the current state.
     uint8_t* d_plane = nullptr;
+    bool two_planes = false;
+    uint32_t plane_par = 0;
     uint8_t* d_danger = nullptr;  // infectious-neighbour counts, same layout as d_plane
     uint32_t* d_claim = nullptr;
     uint32_t* d_counts = nullptr;  // [hour of segment][replicate][8]
@@ -120,6 +125,7 @@ struct epi_engine {
     uint32_t *s_pos = nullptr, *s_wsa = nullptr;
     uint2* s_st = nullptr;
     uint8_t* s_plane = nullptr;
+    uint32_t s_plane_par = 0;
     uint8_t* s_danger = nullptr;
     bool saved = false;
 
@@ -317,8 +323,9 @@ static bool sleep_hour_skipped(uint32_t first_hour, uint32_t k) {
 
 // The k_decide instance of an hour of the day.
 // The k_decide (single world) or k_decide_ens (ensemble) instance of an hour of the day.
-static DecideKernel decide_kernel(uint32_t hod, bool ensemble = false) {
-#define EPI_PICK(HC) (ensemble ? (DecideKernel)k_decide_ens<HC> : (DecideKernel)k_decide<HC>)
+static DecideKernel decide_kernel(uint32_t hod, bool ensemble = false, bool full = false) {
+#define EPI_PICK(HC)                                                                                                 \
+    (ensemble ? (DecideKernel)k_decide_ens<HC> : full ? (DecideKernel)k_decide<HC, true> : (DecideKernel)k_decide<HC>)
     switch (hour_class(hod)) {
         case kHcStart: return EPI_PICK(kHcStart);
         case kHcEnd: return EPI_PICK(kHcEnd);
@@ -331,6 +338,16 @@ static DecideKernel decide_kernel(uint32_t hod, bool ensemble = false) {
 #undef EPI_PICK
 }
 
+// The hours of day 7..22 of a lone world rebuild its plane in the other buffer (k_commit
+// REBUILD), 16 a day, so the buffer that holds the state after hour x is the parity of the
+// number of such hours among 1..x: a function of x mod 24.  The other hours update the
+// current buffer in place.
+static bool rebuild_hour(uint32_t hod) { return hod >= 7u && hod <= 22u; }
+static uint32_t plane_parity(uint32_t hod) { return (hod >= 7u ? std::min(hod, 22u) - 6u : 0u) & 1u; }
+static uint8_t* plane_buf(const epi_engine* h, uint32_t par) {
+    return h->d_plane + (h->two_planes ? (size_t)par * h->plane_bytes : 0u);
+}
+
 static int commit_blocks_for(uint32_t slots, int per_thread = kCommitSlots) {
     const uint32_t per_block = kThreads * (uint32_t)per_thread;
     return (int)std::max<uint32_t>(1u, (slots + per_block - 1) / per_block);
@@ -339,9 +356,10 @@ static int commit_blocks_for(uint32_t slots, int per_thread = kCommitSlots) {
 // k_commit with S slots per thread and round; the sparse instance for the hours of day 0 and
 // 23, where hardly any agent acts.
 using CommitKernel = void (*)(const DevParams*, const uint32_t*, uint32_t, uint32_t*, const uint32_t*, uint8_t*,
-                              uint8_t*, uint32_t*, const uint32_t*, HourArgs, uint64_t);
-static CommitKernel commit_kernel(int slots_per_thread, bool sparse = false) {
-#define EPI_PICK(S) (sparse ? (CommitKernel)k_commit<S, true> : (CommitKernel)k_commit<S, false>)
+                              uint8_t*, uint32_t*, const uint32_t*, HourArgs, uint64_t, uint4*, uint32_t);
+static CommitKernel commit_kernel(int slots_per_thread, bool sparse = false, bool rebuild = false) {
+#define EPI_PICK(S)                                                                                                  \
+    (sparse ? (CommitKernel)k_commit<S, true> : rebuild ? (CommitKernel)k_commit<S, false, true> : (CommitKernel)k_commit<S, false>)
     switch (slots_per_thread) {
         case 1: return EPI_PICK(1);
         case 2: return EPI_PICK(2);
@@ -390,18 +408,25 @@ static int enqueue_piece(epi_engine* h, uint32_t first_hour, uint32_t nh) {
             LAUNCH(kKSleep, CK(launch_hour_kernel(k_sleep, h->grid_blocks, h->stream, (const DevParams*)h->d_params,
                                                   (const uint32_t*)h->d_chunk_rep, n_chunks, h->d_st, ha)));
         } else {
-            const DecideKernel decide = decide_kernel(hod, h->R() > 1);
+            // the plane of the previous hour, and (a lone world's rebuilding hours) the other
+            // buffer, all zero, which k_commit fills before it zeroes the one the hour read
+            const bool rebuild = h->two_planes && rebuild_hour(hod);
+            uint8_t* read_plane = plane_buf(h, plane_parity((hod + 23u) % 24u));
+            uint8_t* next_plane = plane_buf(h, plane_parity(hod));
+            const DecideKernel decide = decide_kernel(hod, h->R() > 1, rebuild);
             LAUNCH(kKDecide, CK(launch_hour_kernel(
                                   decide, h->grid_blocks, h->stream, (const DevParams*)h->d_params,
                                   (const uint32_t*)h->d_chunk_rep, n_chunks, (const uint32_t*)h->d_pos, h->d_st,
                                   (const uint32_t*)h->d_home, (const uint32_t*)h->d_work, h->d_wsa,
-                                  (const uint8_t*)h->d_plane, (const uint8_t*)h->d_danger, h->d_claim, h->d_tgt, h->d_lost,
+                                  (const uint8_t*)read_plane, (const uint8_t*)h->d_danger, h->d_claim, h->d_tgt, h->d_lost,
                                   ha, h->d_err)));
-            const CommitKernel commit = commit_kernel(h->commit_slots, hod == 0u || hod == 23u);
+            const CommitKernel commit = commit_kernel(h->commit_slots, hod == 0u || hod == 23u, rebuild);
             LAUNCH(kKCommit, CK(launch_hour_kernel(commit, h->commit_blocks, h->stream, (const DevParams*)h->d_params,
                                                    (const uint32_t*)h->d_chunk_rep, h->slots, h->d_pos,
-                                                   (const uint32_t*)h->d_tgt, h->d_plane, h->d_danger, h->d_claim,
-                                                   (const uint32_t*)h->d_lost, ha, (uint64_t)h->claim_cells)));
+                                                   (const uint32_t*)h->d_tgt, next_plane, h->d_danger, h->d_claim,
+                                                   (const uint32_t*)h->d_lost, ha, (uint64_t)h->claim_cells,
+                                                   rebuild ? reinterpret_cast<uint4*>(read_plane) : (uint4*)nullptr,
+                                                   (uint32_t)(rebuild ? h->plane_bytes / 16u : 0u))));
         }
         // the run loop's guard after every day boundary but the piece's last hour (the piece
         // end below takes that one)
@@ -493,6 +518,16 @@ static int run_hours_chunk(epi_engine* h, uint32_t first_hour, uint32_t nh) {
     if (h->last_claim_hour >= (int64_t)first_hour)  // loss marks of hours about to run again
         CK(cudaMemsetAsync(h->d_lost, 0xFF, (size_t)h->slots * sizeof(uint32_t), h->stream));
     h->last_claim_hour = (int64_t)first_hour + nh - 1;
+    if (h->two_planes) {  // the chain reads the state after first_hour - 1 from its parity's buffer
+        const uint32_t need = plane_parity((first_hour + 23u) % 24u);
+        if (need != h->plane_par) {  // and the other buffer zero, as a rebuilding hour wants it
+            CK(cudaMemcpyAsync(plane_buf(h, need), plane_buf(h, h->plane_par), h->plane_bytes, cudaMemcpyDeviceToDevice,
+                               h->stream));
+            CK(cudaMemsetAsync(plane_buf(h, h->plane_par), 0, h->plane_bytes, h->stream));
+            h->plane_par = need;
+        }
+    }
+    const bool ran = h->reps[0].active;  // a lone world whose run has ended runs no hour kernel
     const size_t row_words = (size_t)h->R() * 8;
     CK(cudaMemsetAsync(h->d_counts, 0, (size_t)nh * row_words * sizeof(uint32_t), h->stream));
     if (h->stream_file) CK(cudaMemsetAsync(h->d_exc_n, 0, (size_t)nh * sizeof(uint32_t), h->stream));
@@ -532,11 +567,15 @@ static int run_hours_chunk(epi_engine* h, uint32_t first_hour, uint32_t nh) {
     rc = check_error_flag(h);
     if (rc) return rc;
     std::vector<uint8_t> ended(h->R(), 0);  // stop rule met at an earlier hour of this chain
+    int end_row = -1;                       // the first such row (later hours ran no kernel)
     for (uint32_t k = 0; k < nh && h->halt_row < 0; ++k) {
         for (uint32_t r = 0; r < h->R(); ++r) {
             if (!h->reps[r].active || ended[r]) continue;
             const uint32_t* c = h->h_counts + ((size_t)k * h->R() + r) * 8;
-            if (h->stop_rule && c[1] == 0 && c[2] == 0 && c[3] == 0) ended[r] = 1;
+            if (h->stop_rule && c[1] == 0 && c[2] == 0 && c[3] == 0) {
+                ended[r] = 1;
+                if (end_row < 0) end_row = (int)k;
+            }
             const uint64_t total = (uint64_t)c[0] + c[1] + c[2] + c[3] + c[4] + c[5];
             if (total != h->reps[r].n) {  // assert_eq!(csv_record.total(), current_population), allocation_map.rs:128
                 h->err = "replicate " + std::to_string(r) + ": counts total " + std::to_string(total) + " != population " +
@@ -545,6 +584,12 @@ static int run_hours_chunk(epi_engine* h, uint32_t first_hour, uint32_t nh) {
             }
         }
         if (h->stop_rule && h->h_counts[(size_t)k * row_words + 6] != 0u) h->halt_row = (int)k;  // later rows did not run
+    }
+    if (h->two_planes && ran) {  // the buffer of the last hour whose kernels ran
+        uint32_t last = nh - 1;
+        if (h->halt_row >= 0) last = std::min(last, (uint32_t)h->halt_row);
+        if (end_row >= 0) last = std::min(last, (uint32_t)end_row);
+        h->plane_par = plane_parity((first_hour + last) % 24u);
     }
     return EPI_OK;
 }
@@ -977,7 +1022,8 @@ static int engine_init(epi_engine* h, const epi_params* params, const epi_agent_
     CK(cudaMalloc(&h->d_tgt, slots * sizeof(uint32_t)));
     CK(cudaMalloc(&h->d_lost, slots * sizeof(uint32_t)));
     CK(cudaMalloc(&h->d_st, slots * sizeof(uint2)));
-    CK(cudaMalloc(&h->d_plane, h->plane_bytes));
+    h->two_planes = R == 1;
+    CK(cudaMalloc(&h->d_plane, h->plane_bytes * (h->two_planes ? 2u : 1u)));
     CK(cudaMalloc(&h->d_danger, h->plane_bytes));
     CK(cudaMalloc(&h->d_claim, h->claim_cells * sizeof(uint32_t)));
     CK(cudaMalloc(&h->d_seg, sizeof(SegDev)));
@@ -1031,8 +1077,9 @@ static int finish_upload(epi_engine* h) {
     const size_t slots = h->slots;
     CK(cudaMemsetAsync(h->d_tgt, 0xFF, slots * sizeof(uint32_t), h->stream));
     CK(cudaMemsetAsync(h->d_lost, 0xFF, slots * sizeof(uint32_t), h->stream));
-    CK(cudaMemsetAsync(h->d_plane, 0, h->plane_bytes, h->stream));
+    CK(cudaMemsetAsync(h->d_plane, 0, h->plane_bytes * (h->two_planes ? 2u : 1u), h->stream));
     CK(cudaMemsetAsync(h->d_danger, 0, h->plane_bytes, h->stream));
+    h->plane_par = 0;
     CK(cudaMemsetAsync(h->d_claim, 0xFF, h->claim_cells * sizeof(uint32_t), h->stream));
     CK(cudaMemsetAsync(h->d_err, 0, sizeof(int), h->stream));
     int rc = push_params(h);
@@ -1089,11 +1136,12 @@ static int snapshot_replica(epi_engine* h, uint32_t r, epi_agent_record* out, si
 static int check_all(epi_engine* h) {
     CK(cudaMemsetAsync(h->d_scratch, 0, 4 * sizeof(unsigned long long), h->stream));
     LAUNCH(kKCheck, (k_check_agents<<<blocks_for(h->slots), kThreads, 0, h->stream>>>(
-                         h->d_params, h->d_chunk_rep, h->slots, h->d_pos, h->d_st, h->d_plane, h->d_scratch)));
-    LAUNCH(kKCheck, (k_check_plane<<<h->grid_blocks, kThreads, 0, h->stream>>>(h->plane_bytes, h->d_plane,
+                         h->d_params, h->d_chunk_rep, h->slots, h->d_pos, h->d_st, plane_buf(h, h->plane_par),
+                         h->d_scratch)));
+    LAUNCH(kKCheck, (k_check_plane<<<h->grid_blocks, kThreads, 0, h->stream>>>(h->plane_bytes, plane_buf(h, h->plane_par),
                                                                                 h->d_scratch + 1)));
     LAUNCH(kKCheck, (k_check_danger<<<dim3(64, std::min<uint32_t>(h->R(), 4096u)), kThreads, 0, h->stream>>>(
-                         h->d_params, h->R(), h->d_plane, h->d_danger, h->d_scratch + 2)));
+                         h->d_params, h->R(), plane_buf(h, h->plane_par), h->d_danger, h->d_scratch + 2)));
     unsigned long long v[4] = {0, 0, 0, 0};
     CK(cudaMemcpyAsync(v, h->d_scratch, sizeof v, cudaMemcpyDeviceToHost, h->stream));
     CK(cudaStreamSynchronize(h->stream));
@@ -1199,7 +1247,8 @@ static int save_state(epi_engine* h) {
     CK(cudaMemcpyAsync(h->s_pos, h->d_pos, n * sizeof(uint32_t), cudaMemcpyDeviceToDevice, h->stream));
     CK(cudaMemcpyAsync(h->s_wsa, h->d_wsa, n * sizeof(uint32_t), cudaMemcpyDeviceToDevice, h->stream));
     CK(cudaMemcpyAsync(h->s_st, h->d_st, n * sizeof(uint2), cudaMemcpyDeviceToDevice, h->stream));
-    CK(cudaMemcpyAsync(h->s_plane, h->d_plane, h->plane_bytes, cudaMemcpyDeviceToDevice, h->stream));
+    CK(cudaMemcpyAsync(h->s_plane, plane_buf(h, h->plane_par), h->plane_bytes, cudaMemcpyDeviceToDevice, h->stream));
+    h->s_plane_par = h->plane_par;
     CK(cudaMemcpyAsync(h->s_danger, h->d_danger, h->plane_bytes, cudaMemcpyDeviceToDevice, h->stream));
     CK(cudaStreamSynchronize(h->stream));
     for (auto& rep : h->reps) {
@@ -1220,7 +1269,9 @@ static int restore_state(epi_engine* h) {
     CK(cudaMemcpyAsync(h->d_pos, h->s_pos, n * sizeof(uint32_t), cudaMemcpyDeviceToDevice, h->stream));
     CK(cudaMemcpyAsync(h->d_wsa, h->s_wsa, n * sizeof(uint32_t), cudaMemcpyDeviceToDevice, h->stream));
     CK(cudaMemcpyAsync(h->d_st, h->s_st, n * sizeof(uint2), cudaMemcpyDeviceToDevice, h->stream));
-    CK(cudaMemcpyAsync(h->d_plane, h->s_plane, h->plane_bytes, cudaMemcpyDeviceToDevice, h->stream));
+    CK(cudaMemcpyAsync(plane_buf(h, h->s_plane_par), h->s_plane, h->plane_bytes, cudaMemcpyDeviceToDevice, h->stream));
+    if (h->two_planes) CK(cudaMemsetAsync(plane_buf(h, 1u - h->s_plane_par), 0, h->plane_bytes, h->stream));
+    h->plane_par = h->s_plane_par;
     CK(cudaMemcpyAsync(h->d_danger, h->s_danger, h->plane_bytes, cudaMemcpyDeviceToDevice, h->stream));
     CK(cudaMemsetAsync(h->d_tgt, 0xFF, n * sizeof(uint32_t), h->stream));
     CK(cudaMemsetAsync(h->d_lost, 0xFF, n * sizeof(uint32_t), h->stream));
@@ -2040,7 +2091,7 @@ extern "C" int epi_tick_hour_noalloc(const epi_params* params, uint32_t hour, ui
         decide<<<blocks, kThreads, 0, s>>>(d_params, nullptr, n_chunks, pos, st, home, work, work_start_at, plane, nullptr,
                                            d_claim, d_tgt, nullptr, ha, d_err);
         k_commit<kCommitSlots><<<commit_blocks_for(n), kThreads, 0, s>>>(d_params, nullptr, n, pos, d_tgt, plane, nullptr,
-                                                                         d_claim, nullptr, ha, 0ull);
+                                                                         d_claim, nullptr, ha, 0ull, nullptr, 0u);
     }
     NOALLOC_CK(cudaGetLastError());
     int err = 0;

@@ -200,8 +200,10 @@ __global__ void __launch_bounds__(kThreads) k_sleep(const DevParams* __restrict_
 }
 
 // The rules of one agent for the hour (slot valid): proposal, claim, infection update, state
-// and target words.  Returns the agent's counts bin.
-template <int HC>
+// and target words.  Returns the agent's counts bin.  FULL (a lone world with two plane
+// buffers, the hours whose commit rebuilds the plane): every agent's target word names its
+// cell and class.
+template <int HC, bool FULL = false>
 __device__ __forceinline__ uint32_t decide_agent(const DevParams& P, const PlaneView& pl, uint32_t* __restrict__ rclaim,
                                                  uint32_t* __restrict__ wsa, uint2* __restrict__ st,
                                                  uint32_t* __restrict__ tgt, uint32_t* __restrict__ lost, uint32_t slot,
@@ -249,9 +251,9 @@ __device__ __forceinline__ uint32_t decide_agent(const DevParams& P, const Plane
     }
     // the plane byte changes when the agent moves or its class changes (s == s0 keeps it)
     uint32_t t = kNoAction;
-    if (moving || s != s0) {
+    if (moving || s != s0 || FULL) {
         const uint32_t cls0 = cell_class(P, s0), cls = s == s0 ? cls0 : cell_class(P, s);
-        if (moving || cls != cls0) t = encode_target(nc, cls, cls0);
+        if (moving || cls != cls0 || FULL) t = encode_target(nc, cls, cls0);
     }
     tgt[slot] = t;
     if (s != s0 || at != at0) st[slot] = make_uint2(s, at);
@@ -267,7 +269,7 @@ __device__ __forceinline__ uint32_t decide_agent(const DevParams& P, const Plane
 // faster on its own workload.
 constexpr int kEnsembleMinBlocks = 5;
 
-template <int HC, bool ENS>
+template <int HC, bool ENS, bool FULL = false>
 __device__ __forceinline__ void decide_body(const DevParams* __restrict__ Pall, const uint32_t* __restrict__ chunk_rep,
                                             uint32_t n_chunks, const uint32_t* __restrict__ pos, uint2* __restrict__ st,
                                             const uint32_t* __restrict__ home, const uint32_t* __restrict__ work,
@@ -309,8 +311,8 @@ __device__ __forceinline__ void decide_body(const DevParams* __restrict__ Pall, 
                         hosp_known = true;
                     }
                 }
-                const uint32_t bin = valid ? decide_agent<HC>(P, pl, rclaim, wsa, st, tgt, lost, slot, slot, s, at, p,
-                                                              home[slot], work[slot], hour, hod, hosp_first, err)
+                const uint32_t bin = valid ? decide_agent<HC, FULL>(P, pl, rclaim, wsa, st, tgt, lost, slot, slot, s, at, p,
+                                                                    home[slot], work[slot], hour, hod, hosp_first, err)
                                            : 0u;
                 count_into(sh, valid, bin);
             }
@@ -364,9 +366,10 @@ __device__ __forceinline__ void decide_body(const DevParams* __restrict__ Pall, 
         const uint32_t *__restrict__ work, uint32_t *__restrict__ wsa, const uint8_t *__restrict__ plane,             \
         const uint8_t *__restrict__ danger, uint32_t *__restrict__ claim, uint32_t *__restrict__ tgt,                 \
         uint32_t *__restrict__ lost, HourArgs ha, int *err
-template <int HC>
+template <int HC, bool FULL = false>
 __global__ void __launch_bounds__(kThreads) k_decide(EPI_DECIDE_PARAMS) {
-    decide_body<HC, false>(Pall, chunk_rep, n_chunks, pos, st, home, work, wsa, plane, danger, claim, tgt, lost, ha, err);
+    decide_body<HC, false, FULL>(Pall, chunk_rep, n_chunks, pos, st, home, work, wsa, plane, danger, claim, tgt, lost, ha,
+                                 err);
 }
 template <int HC>
 __global__ void __launch_bounds__(kThreads, kEnsembleMinBlocks) k_decide_ens(EPI_DECIDE_PARAMS) {
@@ -383,15 +386,22 @@ __global__ void __launch_bounds__(kThreads, kEnsembleMinBlocks) k_decide_ens(EPI
 // SPARSE (hours of day 0 and 23, where a few agents in a million move or change class) reads
 // the target words first and the position and loss mark only of the slots that act: about
 // 5 us per launch at 1M agents instead of 9-10 us.
+// REBUILD (a lone world with two plane buffers, the hours of day 7..22): `plane` is the other
+// buffer, all zero, and every agent writes its final cell's byte there (one scattered store
+// per agent instead of a cleared and a set byte per mover; k_decide then names every agent's
+// cell and class in its target word).  The launch then zeroes `spent`, the buffer the hour
+// read (clear_words 16-byte words), which the next rebuilding hour fills: nothing reads it
+// any more.
 constexpr int kCommitSlots = 4;   // default S
 constexpr int kMaxCommitSlots = 8;
 
-template <int S, bool SPARSE = false>
+template <int S, bool SPARSE = false, bool REBUILD = false>
 __global__ void __launch_bounds__(kThreads) k_commit(const DevParams* __restrict__ Pall, const uint32_t* __restrict__ chunk_rep,
                                                      uint32_t n_slots, uint32_t* __restrict__ pos,
                                                      const uint32_t* __restrict__ tgt, uint8_t* __restrict__ plane,
                                                      uint8_t* __restrict__ danger, uint32_t* __restrict__ claim,
-                                                     const uint32_t* __restrict__ lost, HourArgs ha, uint64_t clear_cells) {
+                                                     const uint32_t* __restrict__ lost, HourArgs ha, uint64_t clear_cells,
+                                                     uint4* __restrict__ spent, uint32_t clear_words) {
     dep_wait();
     const HourRow hr = hour_row(ha);
     const uint32_t* prev = prev_ptr(ha, hr.row);
@@ -444,9 +454,13 @@ __global__ void __launch_bounds__(kThreads) k_commit(const DevParams* __restrict
             size_t new_cell = old_cell;
             if (win) {
                 new_cell = (size_t)(unpack_y(xy) + 1) * WP + (unpack_x(xy) + 1);
+                pos[slot] = xy;
+            }
+            if (REBUILD) {
+                rplane[new_cell] = (uint8_t)cls;
+            } else if (win) {
                 rplane[old_cell] = 0;
                 rplane[new_cell] = (uint8_t)cls;
-                pos[slot] = xy;
             } else if (cls != cls0) {  // a beaten mover whose class held keeps its byte as it is
                 rplane[old_cell] = (uint8_t)cls;
             }
@@ -460,6 +474,10 @@ __global__ void __launch_bounds__(kThreads) k_commit(const DevParams* __restrict
             }
         }
     }
+    // the spent buffer of a rebuilding hour (not when the world did nothing: it still holds the plane)
+    if (REBUILD && !halted0)
+        for (uint32_t w = blockIdx.x * blockDim.x + threadIdx.x; w < clear_words; w += gridDim.x * blockDim.x)
+            spent[w] = make_uint4(0u, 0u, 0u, 0u);
     // A new claim window (kClaimWindow hours) opens before the next hour that claims (hour of
     // day 0 claims next at 7): every claim plane is reset for it.  Only with loss marks, where
     // this kernel reads no claim.
